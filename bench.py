@@ -1,0 +1,317 @@
+#!/usr/bin/env python
+"""Benchmark: even-odd Wilson Dslash GB/s at 32^3x64 (FP64), one JSON line.
+
+Workload (the plain-FP64 GPU configuration): 32^3x64 lattice, seeded
+synthetic SU(3) links exp(i*0.5*H) (seed 2), unit-norm Gaussian source
+(seed 2).  One step = one even-odd hopping application D_eo over the Vh =
+1,048,576 even sites, on fields resident in HBM.  GB/s counts the compulsory
+bytes of one application: 8 links x 144 B + spinor in 192 B + spinor out
+192 B = 1536 B per output site (FP64).  The inputs (1.2 GB of links, 201 MB
+per spinor parity) are larger than L2 (129 MB), so no flush is needed.
+
+`e2e` measures the same metric through the reference-facing host-buffer
+entry point (wd_host_dslash_offd = DslashoffdNew): every step copies the
+reference-layout source from pinned host memory to the device, converts the
+layout, applies the hopping term, and copies the full destination back.
+
+Multi-GPU: replicas only (the reference's domain decomposition is replaced by
+one lattice per GPU); value = sum over ranks of per-rank work / max time.
+
+--impl reference times the reference's CPU implementation of the same
+application (the oracle's C restatement on all host cores; the reference's
+own AVX2 sources do not build on the Arm host of the GPU machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "ipcc2021-final_gb300"))
+
+DIMS = (32, 32, 32, 64)
+SEED = 2
+EPS = 0.5
+MASS = 0.05
+BYTES_PER_SITE_F64 = 8 * 144 + 192 + 192   # links + spinor in + spinor out
+FLOPS_PER_SITE = 1320
+METRIC = "Dslash GB/s at 32^3x64 (even-odd D_eo, FP64, compulsory bytes)"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = REPO / "profiles" / name
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline_port(gauge, src, dims, seconds: float = 12.0) -> dict:
+    """The oracle's C restatement of DslashoffdNew on all host cores, full lattice,
+    repeated until about `seconds` of CPU work."""
+    sys.path.insert(0, str(REPO / "oracle"))
+    from oracle import Oracle
+
+    orc = Oracle()
+    cores = orc.threads(os.cpu_count() or 1)
+    vh = int(np.prod(dims)) // 2
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        orc.dslash_offd(src, gauge, dims, 0, 0)
+        reps += 1
+        if time.perf_counter() - t0 > seconds or reps >= 50:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": BYTES_PER_SITE_F64 * vh / dt / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"{reps} DslashoffdNew applications at {'x'.join(map(str, dims))} (full workload), "
+                      f"{dt * 1e3:.1f} ms each, C restatement with OpenMP over sites"}
+
+
+def run_reference(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import wilson_gb300 as wd
+
+    gauge = wd.gen_gauge(DIMS, SEED, EPS)
+    src = wd.gen_source(DIMS, SEED)
+    sys.path.insert(0, str(REPO / "oracle"))
+    from oracle import Oracle
+
+    orc = Oracle()
+    cores = orc.threads(os.cpu_count() or 1)
+    vh = int(np.prod(DIMS)) // 2
+    orc.dslash_offd(src, gauge, DIMS, 0, 0)  # warm-up (page in, thread pool)
+    # bounded sample: at most `steps` applications or ~60 s
+    t0 = time.perf_counter()
+    n = 0
+    while n < args.steps and (time.perf_counter() - t0) < 60.0:
+        orc.dslash_offd(src, gauge, DIMS, 0, 0)
+        n += 1
+    dt = (time.perf_counter() - t0) / n
+    v = BYTES_PER_SITE_F64 * vh / dt / 1e9
+    line = {"metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": world, "steps": n, "warmup": args.warmup,
+            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded SU(3) links eps=0.5, Gaussian source)",
+            "config": {"workload": "D_eo FP64 32^3x64, seed 2", "lattice": list(DIMS), "sites": int(np.prod(DIMS)),
+                       "parallelism": "host threads"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "GB/s", "cores": cores, "kind": "port",
+                             "sample": f"{n} DslashoffdNew applications at 32x32x32x64 (C restatement of the "
+                                       f"reference, OpenMP over sites; the reference's AVX2 sources do not "
+                                       f"build on this Arm host)"},
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import wilson_gb300 as wd
+
+    prec = {"f64": wd.F64, "df64": wd.DF64}[args.prec]
+    gauge = wd.gen_gauge(DIMS, SEED, EPS)
+    src = wd.gen_source(DIMS, SEED)
+    vh = int(np.prod(DIMS)) // 2
+    ctx = wd.Context(local)
+    lat = ctx.lattice(DIMS, gauge)
+    fin, fout = lat.field(src), lat.field()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        lat.dslash_eo(fin, fout, 0, 0, prec)
+    ctx.sync()
+
+    clocks = ClockSampler(local)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = ctx.launches
+    e0.record(stream)
+    for _ in range(args.steps):
+        lat.dslash_eo(fin, fout, 0, 0, prec)
+    e1.record(stream)
+    e1.synchronize()
+    launches = ctx.launches - launches0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    t_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * BYTES_PER_SITE_F64 * vh / (t_max * 1e-3) / 1e9
+
+    # e2e through the reference-facing entry point, pinned host buffers
+    h_src = torch.from_numpy(src).pin_memory().numpy()
+    h_dst = torch.empty(src.size, dtype=torch.complex128).pin_memory().numpy()
+    host_gauge = [torch.from_numpy(g).pin_memory().numpy() for g in gauge]
+    ctx.host_dslash_offd(DIMS, host_gauge, h_src, 0, 0)  # first call uploads the links
+    n_e2e = max(3, min(args.steps, 20))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(n_e2e):
+        lib_status = wd.lib.wd_host_dslash_offd(ctx.handle, wd._dims(DIMS), wd._gauge_ptrs(host_gauge),
+                                                wd._ptr(h_src), wd._ptr(h_dst), 0, 0)
+        ctx.check(lib_status)
+    e2e_s = (time.perf_counter() - t0) / n_e2e
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_v = world * BYTES_PER_SITE_F64 * vh / e2e_s / 1e9
+
+    if rank == 0:
+        peak, peak_src = measured_peak_hbm()
+        fp64_peak, fp32_peak = ctx.fma_peak()
+        achieved = BYTES_PER_SITE_F64 * vh / (ms * 1e-3) / 1e9
+        gflops = FLOPS_PER_SITE * vh / (ms * 1e-3) / 1e9
+        traffic = profiled_traffic(f"dslash_{args.prec}_32c64.md")
+        line = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.prec,
+            "data": "synthetic (seeded SU(3) links eps=0.5, unit Gaussian source)",
+            "config": {"workload": "even-odd Dslash D_eo, 32^3x64, seed 2 (1000 repeated applications)",
+                       "lattice": list(DIMS), "sites": int(np.prod(DIMS)), "precision": args.prec,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (1.2 GB links + 201 MB spinor per parity)"},
+            "gflops": gflops * world,
+            "effective_gbs_quda_style": 2880 * vh / (ms * 1e-3) / 1e9,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "note": "FP64 kernels are bounded by the FP64 pipe on GB300; see compute"},
+            "compute": {"bound": "fp64" if args.prec == "f64" else "fp32",
+                        "achieved_tflops": gflops / 1e3,
+                        "fp64_peak_tflops": fp64_peak, "fp32_peak_tflops": fp32_peak,
+                        "fp64_frac": gflops / 1e3 / fp64_peak if args.prec == "f64" else None,
+                        "peak_source": "measured live (wd_diag_fma_peak)"},
+            "e2e": {"value": e2e_v, "unit": "GB/s", "h2d_bytes_per_step": int(src.nbytes),
+                    "d2h_bytes_per_step": int(src.nbytes), "steps": n_e2e,
+                    "path": "wd_host_dslash_offd (DslashoffdNew), pinned host buffers, links resident"},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_port(gauge, src, DIMS)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--prec", choices=["f64", "df64"], default="f64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * wilson_gb300.h -- C ABI of the GB300 (sm_103a) Wilson-fermion Dslash and CG
+ * library.
+ *
+ * Every entry point takes plain pointers and sizes and returns a wd_status.
+ * The host-buffer entry points (wd_host_*) take and return fields in the
+ * reference's layout, so they replace the reference's functions one for one:
+ *
+ *   fermion  psi[(eo*12 + spin*3 + colour)]   complex double, 16-byte entries
+ *   gauge    U[mu][(eo*9 + row*3 + col)]      U_mu(x), link from x to x+mu
+ *   eo       = lex/2 + ((x+y+z+t)&1) * V/2,   lex = x + Lx*(y + Ly*(z + Lz*t))
+ *   dims     = {Lx, Ly, Lz, Lt}; Lx even; periodic boundaries in all directions
+ *
+ * (reference: include/operator.h:56-67, src/lattice_fermion.cpp:15-22,
+ *  src/load_gauge.cpp:141-161).  The handle-based entry points keep gauge and
+ * fermion fields resident in device memory in an even-odd split,
+ * structure-of-arrays layout; layout conversion happens on the device.
+ *
+ * Threading: a context owns one CUDA stream; calls on one context must come
+ * from one host thread at a time.  Different contexts are independent.
+ */
+#ifndef WILSON_GB300_H
+#define WILSON_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum wd_status {
+    WD_OK = 0,
+    WD_ERR_BAD_DIMS = 1,      /* lattice extents invalid (Lx odd, <= 0, too large) */
+    WD_ERR_OOM = 2,           /* device allocation failed or HBM budget exceeded */
+    WD_ERR_NOT_CONVERGED = 3, /* solver reached max iterations */
+    WD_ERR_TIMEOUT = 4,       /* a bounded device wait ran out */
+    WD_ERR_CUDA = 5,          /* CUDA runtime error (see wd_last_error) */
+    WD_ERR_BAD_ARG = 6,       /* null pointer, mismatched lattice, bad enum */
+    WD_ERR_NO_DEVICE = 7,     /* no CUDA device / wrong architecture */
+    WD_ERR_NAN = 8            /* solver produced a non-finite residual */
+} wd_status;
+
+/* Arithmetic used by the hopping kernels. */
+typedef enum wd_precision {
+    WD_PREC_F64 = 0,  /* native FP64 */
+    WD_PREC_DF64 = 1, /* double-float: FP32 hi/lo pairs, ~48-bit mantissa, FP64-class results */
+    WD_PREC_F32 = 2,  /* FP32 storage and arithmetic */
+    WD_PREC_F16 = 3   /* FP16 spinors with a per-site FP32 scale, 12-real links, FP32 arithmetic */
+} wd_precision;
+
+typedef struct wd_context wd_context; /* device, stream, scratch */
+typedef struct wd_lattice wd_lattice; /* lattice extents + resident gauge field */
+typedef struct wd_field wd_field;     /* resident full-lattice spinor field (FP64) */
+
+/* ---- context ---------------------------------------------------------- */
+wd_status wd_context_create(int device, wd_context **ctx);
+void wd_context_destroy(wd_context *ctx);
+const char *wd_status_string(wd_status s);
+/* Text of the last error recorded on this context ("" if none). */
+const char *wd_last_error(const wd_context *ctx);
+/* Wait for all work queued on the context's stream. */
+wd_status wd_context_sync(wd_context *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or overlap work. */
+void *wd_context_stream(wd_context *ctx);
+/* Device kernels launched on this context since creation (bookkeeping for benchmarks). */
+uint64_t wd_context_launches(const wd_context *ctx);
+
+/* ---- gauge field (replaces lattice_gauge, include/lattice_gauge.h:11-26) ---- */
+/* Upload four reference-layout link arrays (each V*9 complex doubles).
+ * The library keeps its own device copy; the host arrays may be freed after. */
+wd_status wd_lattice_create(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                            wd_lattice **lat);
+/* Refresh the device copy of the links from host arrays of the same lattice. */
+wd_status wd_lattice_update(wd_context *ctx, wd_lattice *lat, const double *const gauge[4]);
+void wd_lattice_destroy(wd_lattice *lat);
+/* Sites of the full lattice. */
+int64_t wd_lattice_volume(const wd_lattice *lat);
+
+/* ---- fermion fields (replaces lattice_fermion, include/lattice_fermion.h:12-32) ---- */
+wd_status wd_field_create(wd_context *ctx, const wd_lattice *lat, wd_field **f);
+void wd_field_destroy(wd_field *f);
+/* host: V*12 complex doubles in the reference layout */
+wd_status wd_field_upload(wd_context *ctx, wd_field *f, const double *host);
+wd_status wd_field_download(wd_context *ctx, const wd_field *f, double *host);
+wd_status wd_field_zero(wd_context *ctx, wd_field *f);
+wd_status wd_field_copy(wd_context *ctx, wd_field *dst, const wd_field *src);
+
+/* ---- operators on resident fields ------------------------------------ */
+/* DslashoffdNew (src/dslash_new.cpp:1341) / Dslashoffd (src/dslash.cpp:38):
+ * out[cb] = -1/2 * D_{cb,1-cb} in[1-cb]; out[1-cb] = 0.  dag != 0 gives the
+ * hermitian conjugate hopping term.  prec selects the kernel arithmetic. */
+wd_status wd_dslash_offd(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                         int dag, int cb, wd_precision prec);
+/* The even-odd hopping half-application alone (the unit "one even-odd Dslash"
+ * of the benchmarks; the inner operator of DslashoffdNew, src/dslash_new.cpp:1831-2296):
+ * out[cb] = -1/2 * D_{cb,1-cb} in[1-cb]; out[1-cb] is left untouched. */
+wd_status wd_dslash_eo(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                       int dag, int cb, wd_precision prec);
+/* DslashEEOONew (src/dslash_new.cpp:1301): out = (4+mass) in on all sites. */
+wd_status wd_dslash_eeoo(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                         double mass);
+/* DslashNew / Dslash (src/invert.cpp:123-156): out = M in (dag=0) or M^dag in. */
+wd_status wd_dslash_full(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                         double mass, int dag, wd_precision prec);
+/* norm_2 (include/operator_mpi.h:15): sum |a_i|^2, FP64, deterministic order. */
+wd_status wd_norm2(wd_context *ctx, const wd_field *a, double *out);
+/* vector_p (include/operator_mpi.h:48): sum conj(a_i) b_i -> out[0] + i out[1]. */
+wd_status wd_dot(wd_context *ctx, const wd_field *a, const wd_field *b, double out[2]);
+
+/* ---- solvers --------------------------------------------------------- */
+typedef enum wd_solver_kind {
+    WD_SOLVER_CGNR_REF = 0, /* the reference CGinvert: full-lattice CG on M^dag M x = M^dag b,
+                               absolute stop |r_normal| < tol (src/invert.cpp:25-121) */
+    WD_SOLVER_CG_EO = 1     /* even-odd (Schur) preconditioned CG on the normal equations of
+                               Mhat = a - D_eo D_oe/(4a); relative stop on |b - Mx|/|b| */
+} wd_solver_kind;
+
+typedef struct wd_solver_params {
+    wd_solver_kind kind;
+    double mass;
+    double tol;          /* CGNR_REF: absolute |r|; CG_EO: target relative true residual */
+    int max_iter;
+    wd_precision prec;   /* arithmetic of the inner hopping kernel; FP64/DF64 or mixed F32/F16 */
+    double delta;        /* reliable-update threshold for mixed precision (0 -> 0.1) */
+    int use_initial_guess; /* CG_EO: 1 = start from dest, 0 = start from zero */
+} wd_solver_params;
+
+typedef struct wd_solver_stats {
+    int iterations;        /* CG iterations (inner iterations for mixed precision) */
+    int reliable_updates;  /* FP64 residual recomputations */
+    double residual;       /* solver's final residual as defined by the solver kind */
+    double true_residual;  /* |b - M x| / |b| recomputed in FP64 on the device */
+    double seconds;        /* wall time of the solve on the device stream */
+    int converged;
+} wd_solver_stats;
+
+void wd_solver_params_default(wd_solver_params *p);
+
+/* CGinvert (src/invert.cpp:25-121) on resident fields; dest holds the initial
+ * guess on entry (the reference's own random guess is generated by the C++
+ * compatibility layer with rand(), as src/invert.cpp:42-44 does). */
+wd_status wd_solve(wd_context *ctx, const wd_lattice *lat, const wd_field *src, wd_field *dest,
+                   const wd_solver_params *params, wd_solver_stats *stats);
+
+/* check (src/check.cpp:28-110): out[0]=|b| out[1]=|x| out[2..3]=(Mb,Mb) out[4..5]=(b,M^dag M b)
+ * out[6..7]=(Mx,Mx) out[8..9]=(x,M^dag M x) out[10]=|Mx-b| out[11]=|M^dag M x - M^dag b| */
+wd_status wd_check(wd_context *ctx, const wd_lattice *lat, const wd_field *b, const wd_field *x,
+                   double mass, double out[12]);
+
+/* ---- host-buffer entry points (reference layout in and out) ------------ */
+/* Each uploads its inputs, runs on the device and downloads the result within
+ * the call.  gauge is the reference's U.A[4]. */
+wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                              const double *src, double *dest, int dag, int cb);
+wd_status wd_host_dslash_full(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                              const double *src, double *dest, double mass, int dag);
+/* CGinvert(complex<double>* ...) (src/invert.cpp:15-23).  dest holds the
+ * initial guess on entry and the solution on return. */
+wd_status wd_host_cg(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                     const double *src, double *dest, const wd_solver_params *params,
+                     wd_solver_stats *stats);
+
+/* ---- diagnostics (no counterpart in the reference) ---------------------- */
+/* Measured FMA throughput of this device: FP64 and FP32, in TFLOP/s (an FMA
+ * counts two flops).  Used as the compute roof of the hopping kernels. */
+wd_status wd_diag_fma_peak(wd_context *ctx, double *fp64_tflops, double *fp32_tflops);
+
+/* ---- seeded synthetic inputs (host, deterministic) ---------------------- */
+/* Gauge links U = exp(i eps H) re-unitarised to SU(3), H Gaussian traceless
+ * hermitian; written in the reference layout (4 arrays of V*9 complex). */
+wd_status wd_gen_gauge(const int dims[4], uint64_t seed, double eps, double *const gauge[4]);
+/* Complex Gaussian source on V*12 entries, normalised to unit L2. */
+wd_status wd_gen_source(const int dims[4], uint64_t seed, double *src);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WILSON_GB300_H */

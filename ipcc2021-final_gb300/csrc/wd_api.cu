@@ -1,0 +1,421 @@
+// wd_api.cu -- C ABI: contexts, resident lattices and fields, operators and
+// the host-buffer entry points that replace the reference's functions.
+#include <cstring>
+#include <cstdio>
+#include <string>
+#include "wd_kernels.h"
+#include "wd_precision.h"
+#include "wd_solver.h"
+
+// ------------------------------------------------------------------ errors
+wd_status wd_fail(wd_context *ctx, wd_status s, const std::string &msg)
+{
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+wd_status wd_cuda_check(wd_context *ctx, cudaError_t e, const char *what)
+{
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();  // clear the sticky-free allocation error
+        return wd_fail(ctx, WD_ERR_OOM, m);
+    }
+    return wd_fail(ctx, WD_ERR_CUDA, m);
+}
+
+extern "C" const char *wd_status_string(wd_status s)
+{
+    switch (s) {
+    case WD_OK: return "ok";
+    case WD_ERR_BAD_DIMS: return "bad lattice dimensions";
+    case WD_ERR_OOM: return "out of device memory";
+    case WD_ERR_NOT_CONVERGED: return "solver did not converge";
+    case WD_ERR_TIMEOUT: return "device wait timed out";
+    case WD_ERR_CUDA: return "CUDA error";
+    case WD_ERR_BAD_ARG: return "bad argument";
+    case WD_ERR_NO_DEVICE: return "no usable CUDA device";
+    case WD_ERR_NAN: return "non-finite residual";
+    }
+    return "unknown status";
+}
+
+extern "C" const char *wd_last_error(const wd_context *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+// ----------------------------------------------------------------- context
+extern "C" wd_status wd_context_create(int device, wd_context **out)
+{
+    if (!out) return WD_ERR_BAD_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) {
+        cudaGetLastError();
+        return WD_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return WD_ERR_NO_DEVICE;
+    // the kernels are built for sm_103a only
+    if (prop.major != 10 || prop.minor != 3) return WD_ERR_NO_DEVICE;
+    wd_context *ctx = new wd_context();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaMalloc(&ctx->red_partial, sizeof(double2) * (WD_RED_BLOCKS + WD_RED_SLOTS));
+    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->red_result, sizeof(double2) * WD_RED_SLOTS, 0);
+    if (e != cudaSuccess) {
+        wd_context_destroy(ctx);
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? WD_ERR_OOM : WD_ERR_CUDA;
+    }
+    *out = ctx;
+    return WD_OK;
+}
+
+static void host_cache_drop(wd_context *ctx)
+{
+    for (auto &f : ctx->host_f) {
+        wd_field_destroy(f);
+        f = nullptr;
+    }
+    if (ctx->host_lat) wd_lattice_destroy(ctx->host_lat);
+    ctx->host_lat = nullptr;
+    for (auto &p : ctx->host_gauge_ptr) p = nullptr;
+}
+
+extern "C" void wd_context_destroy(wd_context *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    host_cache_drop(ctx);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->red_partial);
+    cudaFree(ctx->staging);
+    if (ctx->red_result) cudaFreeHost(ctx->red_result);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" wd_status wd_context_sync(wd_context *ctx)
+{
+    if (!ctx) return WD_ERR_BAD_ARG;
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return WD_OK;
+}
+
+extern "C" void *wd_context_stream(wd_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+extern "C" uint64_t wd_context_launches(const wd_context *ctx) { return ctx ? ctx->launches : 0; }
+
+static wd_status ensure_staging(wd_context *ctx, size_t bytes)
+{
+    if (ctx->staging_bytes >= bytes) return WD_OK;
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->staging);
+    ctx->staging = nullptr;
+    ctx->staging_bytes = 0;
+    WD_CUDA(ctx, cudaMalloc(&ctx->staging, bytes));
+    ctx->staging_bytes = bytes;
+    return WD_OK;
+}
+
+// ---------------------------------------------------------------- lattice
+static wd_status make_geom(wd_context *ctx, const int *dims, WdGeom *g, int64_t *vol)
+{
+    if (!dims) return wd_fail(ctx, WD_ERR_BAD_ARG, "dims is null");
+    int64_t v = 1;
+    for (int i = 0; i < 4; ++i) {
+        if (dims[i] <= 0) return wd_fail(ctx, WD_ERR_BAD_DIMS, "lattice extent must be positive");
+        v *= dims[i];
+        g->L[i] = dims[i];
+    }
+    if (dims[0] % 2) return wd_fail(ctx, WD_ERR_BAD_DIMS, "Lx must be even for the even-odd layout");
+    if (v > WD_MAX_SITES) return wd_fail(ctx, WD_ERR_BAD_DIMS, "lattice too large");
+    g->Lxh = dims[0] / 2;
+    g->Vh = (int)(v / 2);
+    *vol = v;
+    return WD_OK;
+}
+
+static wd_status upload_gauge(wd_context *ctx, wd_lattice *lat, const double *const gauge[4])
+{
+    const WdGeom &g = lat->g;
+    const size_t bytes = (size_t)lat->volume * 9 * sizeof(double2);
+    wd_status st = ensure_staging(ctx, bytes);
+    if (st != WD_OK) return st;
+    for (int mu = 0; mu < 4; ++mu) {
+        if (!gauge[mu]) return wd_fail(ctx, WD_ERR_BAD_ARG, "gauge pointer is null");
+        WD_CUDA(ctx, cudaMemcpyAsync(ctx->staging, gauge[mu], bytes, cudaMemcpyHostToDevice, ctx->stream));
+        st = wd_gauge_ref_to_soa(ctx, g, mu, (const double2 *)ctx->staging, lat->gauge);
+        if (st != WD_OK) return st;
+    }
+    wd_lattice_invalidate_derived(lat);
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return WD_OK;
+}
+
+extern "C" wd_status wd_lattice_create(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                                       wd_lattice **out)
+{
+    if (!ctx || !out || !gauge) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    wd_lattice *lat = new wd_lattice();
+    lat->ctx = ctx;
+    wd_status st = make_geom(ctx, dims, &lat->g, &lat->volume);
+    if (st != WD_OK) {
+        delete lat;
+        return st;
+    }
+    cudaError_t e = cudaMalloc(&lat->gauge, (size_t)lat->volume * 4 * 9 * sizeof(double2));
+    if (e != cudaSuccess) {
+        delete lat;
+        return wd_cuda_check(ctx, e, "cudaMalloc(gauge)");
+    }
+    st = upload_gauge(ctx, lat, gauge);
+    if (st != WD_OK) {
+        wd_lattice_destroy(lat);
+        return st;
+    }
+    *out = lat;
+    return WD_OK;
+}
+
+extern "C" wd_status wd_lattice_update(wd_context *ctx, wd_lattice *lat, const double *const gauge[4])
+{
+    if (!ctx || !lat || !gauge) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    return upload_gauge(ctx, lat, gauge);
+}
+
+extern "C" void wd_lattice_destroy(wd_lattice *lat)
+{
+    if (!lat) return;
+    cudaFree(lat->gauge);  // cudaFree waits for work in flight on the device
+    wd_lattice_invalidate_derived(lat);
+    delete lat;
+}
+
+extern "C" int64_t wd_lattice_volume(const wd_lattice *lat) { return lat ? lat->volume : 0; }
+
+// ------------------------------------------------------------------ fields
+extern "C" wd_status wd_field_create(wd_context *ctx, const wd_lattice *lat, wd_field **out)
+{
+    if (!ctx || !lat || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    *out = nullptr;
+    wd_field *f = new wd_field();
+    f->lat = lat;
+    cudaError_t e = cudaMalloc(&f->d, (size_t)lat->volume * 12 * sizeof(double2));
+    if (e != cudaSuccess) {
+        delete f;
+        return wd_cuda_check(ctx, e, "cudaMalloc(field)");
+    }
+    e = cudaMemsetAsync(f->d, 0, (size_t)lat->volume * 12 * sizeof(double2), ctx->stream);
+    if (e != cudaSuccess) {
+        cudaFree(f->d);
+        delete f;
+        return wd_cuda_check(ctx, e, "cudaMemsetAsync(field)");
+    }
+    *out = f;
+    return WD_OK;
+}
+
+extern "C" void wd_field_destroy(wd_field *f)
+{
+    if (!f) return;
+    cudaFree(f->d);  // cudaFree waits for work in flight on the device
+    delete f;
+}
+
+extern "C" wd_status wd_field_upload(wd_context *ctx, wd_field *f, const double *host)
+{
+    if (!ctx || !f || !host) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    const size_t bytes = (size_t)f->lat->volume * 12 * sizeof(double2);
+    wd_status st = ensure_staging(ctx, bytes);
+    if (st != WD_OK) return st;
+    WD_CUDA(ctx, cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    st = wd_spinor_ref_to_soa(ctx, f->lat->g, (const double2 *)ctx->staging, f->d);
+    if (st != WD_OK) return st;
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return WD_OK;
+}
+
+extern "C" wd_status wd_field_download(wd_context *ctx, const wd_field *f, double *host)
+{
+    if (!ctx || !f || !host) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    const size_t bytes = (size_t)f->lat->volume * 12 * sizeof(double2);
+    wd_status st = ensure_staging(ctx, bytes);
+    if (st != WD_OK) return st;
+    st = wd_spinor_soa_to_ref(ctx, f->lat->g, f->d, (double2 *)ctx->staging);
+    if (st != WD_OK) return st;
+    WD_CUDA(ctx, cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return WD_OK;
+}
+
+extern "C" wd_status wd_field_zero(wd_context *ctx, wd_field *f)
+{
+    if (!ctx || !f) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    WD_CUDA(ctx, cudaMemsetAsync(f->d, 0, (size_t)f->lat->volume * 12 * sizeof(double2), ctx->stream));
+    return WD_OK;
+}
+
+extern "C" wd_status wd_field_copy(wd_context *ctx, wd_field *dst, const wd_field *src)
+{
+    if (!ctx || !dst || !src) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if (dst->lat->volume != src->lat->volume) return wd_fail(ctx, WD_ERR_BAD_ARG, "field size mismatch");
+    WD_CUDA(ctx, cudaMemcpyAsync(dst->d, src->d, (size_t)src->lat->volume * 12 * sizeof(double2),
+                                 cudaMemcpyDeviceToDevice, ctx->stream));
+    return WD_OK;
+}
+
+// --------------------------------------------------------------- operators
+static wd_status check_fields(wd_context *ctx, const wd_lattice *lat, const wd_field *a, const wd_field *b)
+{
+    if (!ctx || !lat || !a || !b) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if (a->lat->volume != lat->volume || b->lat->volume != lat->volume)
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "field does not belong to this lattice size");
+    if (a == b) return wd_fail(ctx, WD_ERR_BAD_ARG, "input and output must be different fields");
+    return WD_OK;
+}
+
+// out_cb = alpha * D_{cb,1-cb} in_{1-cb} + beta * x_cb, dispatched on precision.
+wd_status wd_hop(wd_context *ctx, const wd_lattice *lat, const double2 *in_block, double2 *out_block,
+                 const double2 *x_block, int cb, int dag, double alpha, double beta, wd_precision prec)
+{
+    switch (prec) {
+    case WD_PREC_F64: return wd_hop_f64(ctx, lat, in_block, out_block, x_block, cb, dag, alpha, beta);
+    default: return wd_fail(ctx, WD_ERR_BAD_ARG, "precision not available for FP64 fields");
+    }
+}
+
+extern "C" wd_status wd_dslash_offd(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
+                                    wd_field *out, int dag, int cb, wd_precision prec)
+{
+    wd_status st = check_fields(ctx, lat, in, out);
+    if (st != WD_OK) return st;
+    if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
+    const int Vh = lat->g.Vh;
+    const size_t blk = (size_t)12 * Vh;
+    // the reference zeroes the whole destination (src/dslash_new.cpp:1398)
+    WD_CUDA(ctx, cudaMemsetAsync(out->d + (1 - cb) * blk, 0, blk * sizeof(double2), ctx->stream));
+    return wd_hop(ctx, lat, in->d + (1 - cb) * blk, out->d + cb * blk, nullptr, cb, dag, -0.5, 0.0, prec);
+}
+
+extern "C" wd_status wd_dslash_eo(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
+                                  wd_field *out, int dag, int cb, wd_precision prec)
+{
+    wd_status st = check_fields(ctx, lat, in, out);
+    if (st != WD_OK) return st;
+    if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
+    const size_t blk = (size_t)12 * lat->g.Vh;
+    return wd_hop(ctx, lat, in->d + (1 - cb) * blk, out->d + cb * blk, nullptr, cb, dag, -0.5, 0.0, prec);
+}
+
+extern "C" wd_status wd_dslash_eeoo(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
+                                    wd_field *out, double mass)
+{
+    if (!ctx || !lat || !in || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    return wd_blas_scale(ctx, 4.0 + mass, in->d, out->d, lat->volume * 12);
+}
+
+extern "C" wd_status wd_dslash_full(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
+                                    wd_field *out, double mass, int dag, wd_precision prec)
+{
+    wd_status st = check_fields(ctx, lat, in, out);
+    if (st != WD_OK) return st;
+    const size_t blk = (size_t)12 * lat->g.Vh;
+    const double a = 4.0 + mass;
+    for (int cb = 0; cb < 2; ++cb) {
+        st = wd_hop(ctx, lat, in->d + (1 - cb) * blk, out->d + cb * blk, in->d + cb * blk, cb, dag, -0.5, a, prec);
+        if (st != WD_OK) return st;
+    }
+    return WD_OK;
+}
+
+extern "C" wd_status wd_norm2(wd_context *ctx, const wd_field *a, double *out)
+{
+    if (!ctx || !a || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    wd_status st = wd_red_norm2(ctx, a->d, a->lat->volume * 12, 0);
+    if (st != WD_OK) return st;
+    double2 r;
+    st = wd_red_fetch(ctx, 1, &r);
+    *out = r.x;
+    return st;
+}
+
+extern "C" wd_status wd_dot(wd_context *ctx, const wd_field *a, const wd_field *b, double out[2])
+{
+    if (!ctx || !a || !b || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if (a->lat->volume != b->lat->volume) return wd_fail(ctx, WD_ERR_BAD_ARG, "field size mismatch");
+    wd_status st = wd_red_dot(ctx, a->d, b->d, a->lat->volume * 12, 0);
+    if (st != WD_OK) return st;
+    double2 r;
+    st = wd_red_fetch(ctx, 1, &r);
+    out[0] = r.x;
+    out[1] = r.y;
+    return st;
+}
+
+// ------------------------------------------------------- host-buffer path
+// The reference's functions take host arrays on every call.  The device copy
+// of the links is kept between calls and refreshed when the caller passes a
+// different gauge array (pointer identity) or different extents; callers that
+// rewrite a gauge array in place call wd_lattice_update on their own lattice.
+static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *const gauge[4])
+{
+    if (!ctx || !dims || !gauge) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    bool same = ctx->host_lat != nullptr;
+    if (same)
+        for (int i = 0; i < 4; ++i)
+            same = same && ctx->host_lat->g.L[i] == dims[i] && ctx->host_gauge_ptr[i] == gauge[i];
+    if (same) return WD_OK;
+    host_cache_drop(ctx);
+    wd_status st = wd_lattice_create(ctx, dims, gauge, &ctx->host_lat);
+    if (st != WD_OK) return st;
+    for (int i = 0; i < 3; ++i) {
+        st = wd_field_create(ctx, ctx->host_lat, &ctx->host_f[i]);
+        if (st != WD_OK) {
+            host_cache_drop(ctx);
+            return st;
+        }
+    }
+    for (int i = 0; i < 4; ++i) ctx->host_gauge_ptr[i] = gauge[i];
+    return WD_OK;
+}
+
+extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                                         const double *src, double *dest, int dag, int cb)
+{
+    wd_status st = host_prepare(ctx, dims, gauge);
+    if (st != WD_OK) return st;
+    if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if ((st = wd_field_upload(ctx, ctx->host_f[0], src)) != WD_OK) return st;
+    if ((st = wd_dslash_offd(ctx, ctx->host_lat, ctx->host_f[0], ctx->host_f[1], dag, cb, WD_PREC_F64)) != WD_OK)
+        return st;
+    return wd_field_download(ctx, ctx->host_f[1], dest);
+}
+
+extern "C" wd_status wd_host_dslash_full(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                                         const double *src, double *dest, double mass, int dag)
+{
+    wd_status st = host_prepare(ctx, dims, gauge);
+    if (st != WD_OK) return st;
+    if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if ((st = wd_field_upload(ctx, ctx->host_f[0], src)) != WD_OK) return st;
+    if ((st = wd_dslash_full(ctx, ctx->host_lat, ctx->host_f[0], ctx->host_f[1], mass, dag, WD_PREC_F64)) != WD_OK)
+        return st;
+    return wd_field_download(ctx, ctx->host_f[1], dest);
+}
+
+extern "C" wd_status wd_host_cg(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                                const double *src, double *dest, const wd_solver_params *params,
+                                wd_solver_stats *stats)
+{
+    wd_status st = host_prepare(ctx, dims, gauge);
+    if (st != WD_OK) return st;
+    if (!src || !dest || !params) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if ((st = wd_field_upload(ctx, ctx->host_f[0], src)) != WD_OK) return st;
+    if ((st = wd_field_upload(ctx, ctx->host_f[1], dest)) != WD_OK) return st;
+    wd_status solve = wd_solve(ctx, ctx->host_lat, ctx->host_f[0], ctx->host_f[1], params, stats);
+    if (solve != WD_OK && solve != WD_ERR_NOT_CONVERGED) return solve;
+    st = wd_field_download(ctx, ctx->host_f[1], dest);
+    return st != WD_OK ? st : solve;
+}

@@ -1,0 +1,70 @@
+// wd_dslash_f64.cu -- native FP64 hopping kernel (the plain drop-in arithmetic).
+//
+// Storage: double2 planes, spinor [12][Vh] per parity, links [mu][parity][9][Vh].
+// Algorithmic traffic per output site: 8 links x 144 B + 1 spinor in x 192 B
+// + 1 spinor out x 192 B = 1536 B (+192 B when the epilogue reads x).
+// Arithmetic: 1320 flop per site.  On GB300 the FP64 pipe (~1.2 TFLOP/s
+// measured) rather than HBM bounds this kernel; wd_dslash_df.cu holds the
+// double-float variant that moves the arithmetic onto the FP32 pipe.
+#include "wd_hop.cuh"
+#include "wd_kernels.h"
+
+namespace {
+
+struct HopF64 {
+    using C = double2;
+    static constexpr int kThreads = 128;
+    WdGeom g;
+    int cb;
+    const double2 *__restrict__ in;     // parity 1-cb block [12][Vh]
+    const double2 *__restrict__ gauge;  // [4][2][9][Vh]
+    const double2 *__restrict__ x;      // parity cb block or null
+    double2 *__restrict__ out;          // parity cb block
+    double alpha, beta;
+
+    __device__ __forceinline__ void load_in(int s, C *v) const
+    {
+#pragma unroll
+        for (int c = 0; c < 12; ++c) v[c] = in[(size_t)c * g.Vh + s];
+    }
+    __device__ __forceinline__ void load_link(int mu, int par, int s, C *U) const
+    {
+        const double2 *b = gauge + (size_t)((mu * 2 + par) * 9) * g.Vh + s;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) U[k] = b[(size_t)k * g.Vh];
+    }
+    __device__ __forceinline__ void epilogue(int s, const C *acc) const
+    {
+        if (x) {
+#pragma unroll
+            for (int c = 0; c < 12; ++c)
+                out[(size_t)c * g.Vh + s] = c_axpby(alpha, acc[c], beta, x[(size_t)c * g.Vh + s]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 12; ++c) out[(size_t)c * g.Vh + s] = c_scale(acc[c], alpha);
+        }
+    }
+};
+
+}  // namespace
+
+wd_status wd_hop_f64(wd_context *ctx, const wd_lattice *lat, const double2 *in_block,
+                     double2 *out_block, const double2 *x_block, int cb, int dag, double alpha,
+                     double beta)
+{
+    HopF64 p;
+    p.g = lat->g;
+    p.cb = cb;
+    p.in = in_block;
+    p.gauge = lat->gauge;
+    p.x = x_block;
+    p.out = out_block;
+    p.alpha = alpha;
+    p.beta = beta;
+    const int threads = HopF64::kThreads;
+    const int blocks = (lat->g.Vh + threads - 1) / threads;
+    if (dag) wd_hop_kernel<true><<<blocks, threads, 0, ctx->stream>>>(p);
+    else wd_hop_kernel<false><<<blocks, threads, 0, ctx->stream>>>(p);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}

@@ -1,0 +1,137 @@
+// wd_hop.cuh -- the Wilson hopping term, written once for every arithmetic
+// type.  One thread computes one output site of parity cb:
+//
+//   acc = sum_mu [ (1 - s g_mu) U_mu(x) psi(x+mu) + (1 + s g_mu) U_mu(x-mu)^dag psi(x-mu) ]
+//   out = alpha * acc + beta * x            (x: same-parity field, optional)
+//
+// s = +1 for D, -1 for D^dag.  The reference's -1/2 (src/dslash.cpp:544-873)
+// is alpha = -0.5; the diagonal (4+m) term of DslashNew is beta.  Neighbours
+// wrap periodically inside the kernel, replacing the reference's halo
+// exchange (src/dslash_new.cpp:1416-1826, 2304-2654).
+//
+// A policy class P supplies the storage format: the complex arithmetic type
+// P::C, loads of a neighbour spinor and of a link matrix, and the epilogue.
+#pragma once
+#include "wd_internal.cuh"
+#include "wd_complex.cuh"
+
+template <int SG, class C>
+__device__ __forceinline__ C wd_addsg(const C &a, const C &b)
+{
+    if constexpr (SG > 0) return c_add(a, b);
+    else return c_sub(a, b);
+}
+
+// Spin projection psi -> (h0, h1) for direction MU, sign SG (see wd_internal.cuh).
+template <int MU, int SG, class C>
+__device__ __forceinline__ void wd_proj(const C *sp, C *h0, C *h1)
+{
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const C s0 = sp[k], s1 = sp[3 + k], s2 = sp[6 + k], s3 = sp[9 + k];
+        if constexpr (MU == 0) {
+            h0[k] = wd_addsg<SG>(s0, c_i(s3));
+            h1[k] = wd_addsg<SG>(s1, c_i(s2));
+        } else if constexpr (MU == 1) {
+            h0[k] = wd_addsg<-SG>(s0, s3);
+            h1[k] = wd_addsg<SG>(s1, s2);
+        } else if constexpr (MU == 2) {
+            h0[k] = wd_addsg<SG>(s0, c_i(s2));
+            h1[k] = wd_addsg<-SG>(s1, c_i(s3));
+        } else {
+            h0[k] = wd_addsg<SG>(s0, s2);
+            h1[k] = wd_addsg<SG>(s1, s3);
+        }
+    }
+}
+
+// Accumulate (t0, t1) = W (h0, h1) into the four spin components.
+template <int MU, int SG, class C>
+__device__ __forceinline__ void wd_recon(const C *t0, const C *t1, C *acc)
+{
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        acc[a] = c_add(acc[a], t0[a]);
+        acc[3 + a] = c_add(acc[3 + a], t1[a]);
+        if constexpr (MU == 0) {
+            acc[6 + a] = wd_addsg<-SG>(acc[6 + a], c_i(t1[a]));
+            acc[9 + a] = wd_addsg<-SG>(acc[9 + a], c_i(t0[a]));
+        } else if constexpr (MU == 1) {
+            acc[6 + a] = wd_addsg<SG>(acc[6 + a], t1[a]);
+            acc[9 + a] = wd_addsg<-SG>(acc[9 + a], t0[a]);
+        } else if constexpr (MU == 2) {
+            acc[6 + a] = wd_addsg<-SG>(acc[6 + a], c_i(t0[a]));
+            acc[9 + a] = wd_addsg<SG>(acc[9 + a], c_i(t1[a]));
+        } else {
+            acc[6 + a] = wd_addsg<SG>(acc[6 + a], t0[a]);
+            acc[9 + a] = wd_addsg<SG>(acc[9 + a], t1[a]);
+        }
+    }
+}
+
+// One of the eight neighbour terms.
+template <int MU, bool FWD, bool DAG, class P>
+__device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, typename P::C *acc)
+{
+    using C = typename P::C;
+    constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
+    const int nb = wd_neighbour(p.g, s, c, MU, FWD);
+    C sp[12];
+    p.load_in(nb, sp);
+    C h0[3], h1[3];
+    wd_proj<MU, SG>(sp, h0, h1);
+    C U[9];
+    // forward: U_mu(x) stored at this site (parity cb);
+    // backward: U_mu(x - mu) stored at the neighbour (parity 1-cb)
+    if constexpr (FWD) p.load_link(MU, p.cb, s, U);
+    else p.load_link(MU, 1 - p.cb, nb, U);
+    C t0[3], t1[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if constexpr (FWD) {
+            t0[a] = c_mul(U[a * 3 + 0], h0[0]);
+            t1[a] = c_mul(U[a * 3 + 0], h1[0]);
+#pragma unroll
+            for (int b = 1; b < 3; ++b) {
+                t0[a] = c_madd(t0[a], U[a * 3 + b], h0[b]);
+                t1[a] = c_madd(t1[a], U[a * 3 + b], h1[b]);
+            }
+        } else {
+            t0[a] = c_mulc(U[a], h0[0]);
+            t1[a] = c_mulc(U[a], h1[0]);
+#pragma unroll
+            for (int b = 1; b < 3; ++b) {
+                t0[a] = c_maddc(t0[a], U[b * 3 + a], h0[b]);
+                t1[a] = c_maddc(t1[a], U[b * 3 + a], h1[b]);
+            }
+        }
+    }
+    wd_recon<MU, SG>(t0, t1, acc);
+}
+
+template <bool DAG, class P>
+__device__ __forceinline__ void wd_hop_site(const P &p, int s, typename P::C *acc)
+{
+    using C = typename P::C;
+    const WdSite c = wd_site(p.g, s, p.cb);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) acc[k] = c_zero(C());
+    wd_hop_dir<0, true, DAG>(p, s, c, acc);
+    wd_hop_dir<0, false, DAG>(p, s, c, acc);
+    wd_hop_dir<1, true, DAG>(p, s, c, acc);
+    wd_hop_dir<1, false, DAG>(p, s, c, acc);
+    wd_hop_dir<2, true, DAG>(p, s, c, acc);
+    wd_hop_dir<2, false, DAG>(p, s, c, acc);
+    wd_hop_dir<3, true, DAG>(p, s, c, acc);
+    wd_hop_dir<3, false, DAG>(p, s, c, acc);
+}
+
+template <bool DAG, class P>
+__global__ void __launch_bounds__(P::kThreads) wd_hop_kernel(const P p)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= p.g.Vh) return;
+    typename P::C acc[12];
+    wd_hop_site<DAG>(p, s, acc);
+    p.epilogue(s, acc);
+}

@@ -1,0 +1,332 @@
+"""Python binding of libwilson_gb300 (ctypes over the C ABI in include/wilson_gb300.h).
+
+Fields cross the boundary as numpy complex128 arrays in the reference layout:
+fermions have V*12 entries (eo*12 + spin*3 + colour), gauge fields are four
+arrays of V*9 entries (eo*9 + row*3 + col), V = Lx*Ly*Lz*Lt with Lx even.
+
+The compute path is the CUDA library only: if it is not built, importing
+this module raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libwilson_gb300.so"
+
+# wd_status
+OK, BAD_DIMS, OOM, NOT_CONVERGED, TIMEOUT, CUDA_ERROR, BAD_ARG, NO_DEVICE, NAN = range(9)
+# wd_precision
+F64, DF64, F32, F16 = range(4)
+# wd_solver_kind
+CGNR_REF, CG_EO = range(2)
+
+
+class WilsonError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+class SolverParams(C.Structure):
+    _fields_ = [("kind", C.c_int), ("mass", C.c_double), ("tol", C.c_double), ("max_iter", C.c_int),
+                ("prec", C.c_int), ("delta", C.c_double), ("use_initial_guess", C.c_int)]
+
+
+class SolverStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("reliable_updates", C.c_int), ("residual", C.c_double),
+                ("true_residual", C.c_double), ("seconds", C.c_double), ("converged", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is not built; run __graft_entry__.build() first")
+    lib = C.CDLL(str(LIB_PATH))
+    vp, ip, dp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double)
+    d4 = C.POINTER(C.c_void_p)
+    sigs = {
+        "wd_context_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
+        "wd_context_destroy": (None, [vp]),
+        "wd_status_string": (C.c_char_p, [C.c_int]),
+        "wd_last_error": (C.c_char_p, [vp]),
+        "wd_context_sync": (C.c_int, [vp]),
+        "wd_context_stream": (vp, [vp]),
+        "wd_context_launches": (C.c_uint64, [vp]),
+        "wd_lattice_create": (C.c_int, [vp, ip, d4, C.POINTER(vp)]),
+        "wd_lattice_update": (C.c_int, [vp, vp, d4]),
+        "wd_lattice_destroy": (None, [vp]),
+        "wd_lattice_volume": (C.c_int64, [vp]),
+        "wd_field_create": (C.c_int, [vp, vp, C.POINTER(vp)]),
+        "wd_field_destroy": (None, [vp]),
+        "wd_field_upload": (C.c_int, [vp, vp, vp]),
+        "wd_field_download": (C.c_int, [vp, vp, vp]),
+        "wd_field_zero": (C.c_int, [vp, vp]),
+        "wd_field_copy": (C.c_int, [vp, vp, vp]),
+        "wd_dslash_offd": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]),
+        "wd_dslash_eo": (C.c_int, [vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]),
+        "wd_dslash_eeoo": (C.c_int, [vp, vp, vp, vp, C.c_double]),
+        "wd_diag_fma_peak": (C.c_int, [vp, dp, dp]),
+        "wd_dslash_full": (C.c_int, [vp, vp, vp, vp, C.c_double, C.c_int, C.c_int]),
+        "wd_norm2": (C.c_int, [vp, vp, dp]),
+        "wd_dot": (C.c_int, [vp, vp, vp, dp]),
+        "wd_solver_params_default": (None, [C.POINTER(SolverParams)]),
+        "wd_solve": (C.c_int, [vp, vp, vp, vp, C.POINTER(SolverParams), C.POINTER(SolverStats)]),
+        "wd_check": (C.c_int, [vp, vp, vp, vp, C.c_double, dp]),
+        "wd_host_dslash_offd": (C.c_int, [vp, ip, d4, vp, vp, C.c_int, C.c_int]),
+        "wd_host_dslash_full": (C.c_int, [vp, ip, d4, vp, vp, C.c_double, C.c_int]),
+        "wd_host_cg": (C.c_int, [vp, ip, d4, vp, vp, C.POINTER(SolverParams), C.POINTER(SolverStats)]),
+        "wd_gen_gauge": (C.c_int, [ip, C.c_uint64, C.c_double, d4]),
+        "wd_gen_source": (C.c_int, [ip, C.c_uint64, vp]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+lib = _load()
+
+# every symbol the public header declares (checked by the CPU tests)
+HEADER = _HERE.parent.parent / "include" / "wilson_gb300.h"
+
+
+def _dims(dims) -> C.Array:
+    d = [int(v) for v in dims]
+    if len(d) != 4:
+        raise ValueError("dims must have 4 entries (Lx, Ly, Lz, Lt)")
+    return (C.c_int * 4)(*d)
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    if a.dtype != np.complex128 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous complex128 array")
+    return C.c_void_p(a.ctypes.data)
+
+
+def _gauge_ptrs(gauge) -> C.Array:
+    if len(gauge) != 4:
+        raise ValueError("gauge must be four arrays (one per direction)")
+    return (C.c_void_p * 4)(*[_ptr(g).value for g in gauge])
+
+
+def volume(dims) -> int:
+    return int(np.prod([int(v) for v in dims]))
+
+
+def gen_gauge(dims, seed: int, eps: float = 0.5) -> list[np.ndarray]:
+    """Seeded SU(3) links exp(i eps H) in the reference layout (4 arrays of V*9)."""
+    V = volume(dims)
+    g = [np.empty(V * 9, np.complex128) for _ in range(4)]
+    _check(lib.wd_gen_gauge(_dims(dims), seed, eps, _gauge_ptrs(g)), None)
+    return g
+
+
+def gen_source(dims, seed: int) -> np.ndarray:
+    """Seeded complex Gaussian source (V*12), unit L2 norm."""
+    s = np.empty(volume(dims) * 12, np.complex128)
+    _check(lib.wd_gen_source(_dims(dims), seed, _ptr(s)), None)
+    return s
+
+
+def _check(status: int, ctx) -> None:
+    if status != OK:
+        detail = lib.wd_last_error(ctx.handle).decode() if ctx is not None else ""
+        raise WilsonError(status, f"{lib.wd_status_string(status).decode()}: {detail}")
+
+
+class Context:
+    """One device + one CUDA stream.  Owns lattices and fields created from it."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        st = lib.wd_context_create(device, C.byref(h))
+        if st != OK:
+            raise WilsonError(st, lib.wd_status_string(st).decode())
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            lib.wd_context_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, status: int) -> None:
+        _check(status, self)
+
+    def sync(self) -> None:
+        self.check(lib.wd_context_sync(self.handle))
+
+    @property
+    def stream(self) -> int:
+        return lib.wd_context_stream(self.handle) or 0
+
+    @property
+    def launches(self) -> int:
+        return int(lib.wd_context_launches(self.handle))
+
+    def fma_peak(self) -> tuple[float, float]:
+        """Measured (FP64, FP32) FMA throughput of the device in TFLOP/s."""
+        a, b = C.c_double(), C.c_double()
+        self.check(lib.wd_diag_fma_peak(self.handle, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def lattice(self, dims, gauge) -> "Lattice":
+        return Lattice(self, dims, gauge)
+
+    # host-buffer entry points (reference layout in and out)
+    def host_dslash_offd(self, dims, gauge, src: np.ndarray, dag: bool, cb: int) -> np.ndarray:
+        out = np.empty_like(src)
+        self.check(lib.wd_host_dslash_offd(self.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(src), _ptr(out),
+                                           int(dag), int(cb)))
+        return out
+
+    def host_dslash_full(self, dims, gauge, src: np.ndarray, mass: float, dag: bool) -> np.ndarray:
+        out = np.empty_like(src)
+        self.check(lib.wd_host_dslash_full(self.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(src), _ptr(out),
+                                           float(mass), int(dag)))
+        return out
+
+    def host_cg(self, dims, gauge, src: np.ndarray, dest: np.ndarray, params: SolverParams,
+                allow_unconverged: bool = False) -> SolverStats:
+        stats = SolverStats()
+        st = lib.wd_host_cg(self.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(src), _ptr(dest), C.byref(params),
+                            C.byref(stats))
+        if not (allow_unconverged and st == NOT_CONVERGED):
+            self.check(st)
+        return stats
+
+
+class Lattice:
+    """Lattice extents plus the resident gauge field."""
+
+    def __init__(self, ctx: Context, dims, gauge):
+        self.ctx = ctx
+        self.dims = tuple(int(v) for v in dims)
+        self.V = volume(dims)
+        h = C.c_void_p()
+        ctx.check(lib.wd_lattice_create(ctx.handle, _dims(dims), _gauge_ptrs(gauge), C.byref(h)))
+        self.handle = h
+
+    def update(self, gauge) -> None:
+        self.ctx.check(lib.wd_lattice_update(self.ctx.handle, self.handle, _gauge_ptrs(gauge)))
+
+    def close(self) -> None:
+        if self.handle:
+            lib.wd_lattice_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def field(self, host: np.ndarray | None = None) -> "Field":
+        f = Field(self)
+        if host is not None:
+            f.upload(host)
+        return f
+
+    # operators
+    def dslash_offd(self, src: "Field", dest: "Field", dag: bool, cb: int, prec: int = F64) -> None:
+        self.ctx.check(lib.wd_dslash_offd(self.ctx.handle, self.handle, src.handle, dest.handle, int(dag), int(cb),
+                                          int(prec)))
+
+    def dslash_eo(self, src: "Field", dest: "Field", dag: bool, cb: int, prec: int = F64) -> None:
+        self.ctx.check(lib.wd_dslash_eo(self.ctx.handle, self.handle, src.handle, dest.handle, int(dag), int(cb),
+                                        int(prec)))
+
+    def dslash_eeoo(self, src: "Field", dest: "Field", mass: float) -> None:
+        self.ctx.check(lib.wd_dslash_eeoo(self.ctx.handle, self.handle, src.handle, dest.handle, float(mass)))
+
+    def dslash_full(self, src: "Field", dest: "Field", mass: float, dag: bool, prec: int = F64) -> None:
+        self.ctx.check(lib.wd_dslash_full(self.ctx.handle, self.handle, src.handle, dest.handle, float(mass),
+                                          int(dag), int(prec)))
+
+    def solve(self, src: "Field", dest: "Field", params: SolverParams, allow_unconverged: bool = False) -> SolverStats:
+        stats = SolverStats()
+        st = lib.wd_solve(self.ctx.handle, self.handle, src.handle, dest.handle, C.byref(params), C.byref(stats))
+        if not (allow_unconverged and st == NOT_CONVERGED):
+            self.ctx.check(st)
+        return stats
+
+    def check(self, b: "Field", x: "Field", mass: float) -> np.ndarray:
+        out = np.zeros(12, np.float64)
+        self.ctx.check(lib.wd_check(self.ctx.handle, self.handle, b.handle, x.handle, float(mass),
+                                    out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+
+class Field:
+    """Resident FP64 spinor field over the full lattice."""
+
+    def __init__(self, lat: Lattice):
+        self.lat = lat
+        h = C.c_void_p()
+        lat.ctx.check(lib.wd_field_create(lat.ctx.handle, lat.handle, C.byref(h)))
+        self.handle = h
+
+    def upload(self, host: np.ndarray) -> None:
+        if host.size != self.lat.V * 12:
+            raise ValueError("field size mismatch")
+        self.lat.ctx.check(lib.wd_field_upload(self.lat.ctx.handle, self.handle, _ptr(host)))
+
+    def download(self) -> np.ndarray:
+        out = np.empty(self.lat.V * 12, np.complex128)
+        self.lat.ctx.check(lib.wd_field_download(self.lat.ctx.handle, self.handle, _ptr(out)))
+        return out
+
+    def zero(self) -> None:
+        self.lat.ctx.check(lib.wd_field_zero(self.lat.ctx.handle, self.handle))
+
+    def copy_from(self, other: "Field") -> None:
+        self.lat.ctx.check(lib.wd_field_copy(self.lat.ctx.handle, self.handle, other.handle))
+
+    def norm2(self) -> float:
+        v = C.c_double()
+        self.lat.ctx.check(lib.wd_norm2(self.lat.ctx.handle, self.handle, C.byref(v)))
+        return v.value
+
+    def dot(self, other: "Field") -> complex:
+        v = (C.c_double * 2)()
+        self.lat.ctx.check(lib.wd_dot(self.lat.ctx.handle, self.handle, other.handle, v))
+        return complex(v[0], v[1])
+
+    def close(self) -> None:
+        if self.handle:
+            lib.wd_field_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solver_params(kind: int = CG_EO, mass: float = 0.1, tol: float = 1e-10, max_iter: int = 1000,
+                  prec: int = F64, delta: float = 0.1, use_initial_guess: bool = False) -> SolverParams:
+    p = SolverParams()
+    lib.wd_solver_params_default(C.byref(p))
+    p.kind, p.mass, p.tol, p.max_iter, p.prec, p.delta = kind, mass, tol, max_iter, prec, delta
+    p.use_initial_guess = int(use_initial_guess)
+    return p
