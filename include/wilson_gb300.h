@@ -161,6 +161,21 @@ wd_status wd_host_cg(wd_context *ctx, const int dims[4], const double *const gau
                      const double *src, double *dest, const wd_solver_params *params,
                      wd_solver_stats *stats);
 
+/* ---- allocation-free dot product (no counterpart in the reference) ------- */
+/* sum_i conj(a_i) b_i over n complex doubles, for callers that cannot
+ * allocate device memory: codes that hand all of HBM to their own pool, and
+ * latency-critical loops that must not call cudaMalloc/cudaFree (both
+ * synchronise the device).  a and b are device pointers (16-byte aligned) to
+ * n interleaved (re, im) pairs; out is a device pointer (8-byte aligned) that
+ * receives re, im.  Work is queued on `stream` (a cudaStream_t, NULL = the
+ * default stream); the call itself allocates nothing.
+ * Limit: n <= 134217728 (32768 partial sums of 4096 entries in a fixed 512 KiB
+ * device array that every GPU loading the library keeps until exit); larger n
+ * returns WD_ERR_BAD_ARG.  The first call on a device looks up that array's
+ * device address and should come before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU race and give undefined results. */
+wd_status wd_dot_noalloc(const double *a, const double *b, int64_t n, double *out, void *stream);
+
 /* ---- diagnostics (no counterpart in the reference) ---------------------- */
 /* Measured FMA throughput of this device: FP64 and FP32, in TFLOP/s (an FMA
  * counts two flops).  Used as the compute roof of the hopping kernels. */
