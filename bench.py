@@ -201,11 +201,12 @@ def run_ours(args) -> None:
     import wilson_gb300 as wd
 
     prec = {"f64": wd.F64, "df64": wd.DF64}[args.prec]
-    gauge = wd.gen_gauge(DIMS, SEED, EPS)
-    src = wd.gen_source(DIMS, SEED)
-    vh = int(np.prod(DIMS)) // 2
+    dims = tuple(args.dims)
+    gauge = wd.gen_gauge(dims, SEED, EPS)
+    src = wd.gen_source(dims, SEED)
+    vh = int(np.prod(dims)) // 2
     ctx = wd.Context(local)
-    lat = ctx.lattice(DIMS, gauge)
+    lat = ctx.lattice(dims, gauge)
     fin, fout = lat.field(src), lat.field()
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
 
@@ -240,23 +241,26 @@ def run_ours(args) -> None:
     value = world * BYTES_PER_SITE_F64 * vh / (t_max * 1e-3) / 1e9
 
     # e2e through the reference-facing entry point, pinned host buffers
-    h_src = torch.from_numpy(src).pin_memory().numpy()
-    h_dst = torch.empty(src.size, dtype=torch.complex128).pin_memory().numpy()
-    host_gauge = [torch.from_numpy(g).pin_memory().numpy() for g in gauge]
-    ctx.host_dslash_offd(DIMS, host_gauge, h_src, 0, 0)  # first call uploads the links
-    n_e2e = max(3, min(args.steps, 20))
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(n_e2e):
-        lib_status = wd.lib.wd_host_dslash_offd(ctx.handle, wd._dims(DIMS), wd._gauge_ptrs(host_gauge),
-                                                wd._ptr(h_src), wd._ptr(h_dst), 0, 0)
-        ctx.check(lib_status)
-    e2e_s = (time.perf_counter() - t0) / n_e2e
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_v = world * BYTES_PER_SITE_F64 * vh / e2e_s / 1e9
+    e2e = None
+    if not args.no_e2e:
+        h_src = torch.from_numpy(src).pin_memory().numpy()
+        h_dst = torch.empty(src.size, dtype=torch.complex128).pin_memory().numpy()
+        host_gauge = [torch.from_numpy(g).pin_memory().numpy() for g in gauge]
+        ctx.host_dslash_offd(dims, host_gauge, h_src, 0, 0)  # first call uploads the links
+        n_e2e = max(3, min(args.steps, 20))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            ctx.check(wd.lib.wd_host_dslash_offd(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
+                                                 wd._ptr(h_src), wd._ptr(h_dst), 0, 0))
+        e2e_s = (time.perf_counter() - t0) / n_e2e
+        if world > 1:
+            t = torch.tensor([e2e_s], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": world * BYTES_PER_SITE_F64 * vh / e2e_s / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": int(src.nbytes), "d2h_bytes_per_step": int(src.nbytes), "steps": n_e2e,
+               "path": "wd_host_dslash_offd (DslashoffdNew), pinned host buffers, links resident"}
 
     if rank == 0:
         peak, peak_src = measured_peak_hbm()
@@ -269,8 +273,9 @@ def run_ours(args) -> None:
             "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.prec,
             "data": "synthetic (seeded SU(3) links eps=0.5, unit Gaussian source)",
-            "config": {"workload": "even-odd Dslash D_eo, 32^3x64, seed 2 (1000 repeated applications)",
-                       "lattice": list(DIMS), "sites": int(np.prod(DIMS)), "precision": args.prec,
+            "config": {"workload": f"even-odd Dslash D_eo, {'x'.join(map(str, dims))}, seed 2 "
+                                   f"({args.steps} repeated applications)",
+                       "lattice": list(dims), "sites": int(np.prod(dims)), "precision": args.prec,
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (1.2 GB links + 201 MB spinor per parity)"},
             "gflops": gflops * world,
@@ -283,14 +288,12 @@ def run_ours(args) -> None:
                         "fp64_peak_tflops": fp64_peak, "fp32_peak_tflops": fp32_peak,
                         "fp64_frac": gflops / 1e3 / fp64_peak if args.prec == "f64" else None,
                         "peak_source": "measured live (wd_diag_fma_peak)"},
-            "e2e": {"value": e2e_v, "unit": "GB/s", "h2d_bytes_per_step": int(src.nbytes),
-                    "d2h_bytes_per_step": int(src.nbytes), "steps": n_e2e,
-                    "path": "wd_host_dslash_offd (DslashoffdNew), pinned host buffers, links resident"},
+            "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clk,
         }
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline_port(gauge, src, DIMS)
+            line["cpu_baseline"] = cpu_baseline_port(gauge, src, dims)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -304,6 +307,9 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--prec", choices=["f64", "df64"], default="f64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--dims", type=int, nargs=4, default=list(DIMS),
+                    help="lattice extents (default 32 32 32 64, the benchmark configuration)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
