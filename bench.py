@@ -42,6 +42,10 @@ SEED = 2
 EPS = 0.5
 MASS = 0.05
 BYTES_PER_SITE_F64 = 8 * 144 + 192 + 192   # links + spinor in + spinor out
+# compulsory bytes per output site of one D_eo in each storage format:
+# f64 / df64: 18-real links 144 B, spinor 192 B; f32: 12-real links 48 B,
+# spinor 96 B; f16: 12-real links 24 B, spinor 48 B + 4 B scale
+BYTES_PER_SITE = {"f64": 1536, "df64": 1536, "f32": 8 * 48 + 96 + 96, "f16": 8 * 24 + 52 + 52}
 FLOPS_PER_SITE = 1320
 METRIC = "Dslash GB/s at 32^3x64 (even-odd D_eo, FP64, compulsory bytes)"
 
@@ -200,14 +204,15 @@ def run_ours(args) -> None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import wilson_gb300 as wd
 
-    prec = {"f64": wd.F64, "df64": wd.DF64}[args.prec]
+    prec = {"f64": wd.F64, "df64": wd.DF64, "f32": wd.F32, "f16": wd.F16}[args.prec]
+    bps = BYTES_PER_SITE[args.prec]
     dims = tuple(args.dims)
     gauge = wd.gen_gauge(dims, SEED, EPS)
     src = wd.gen_source(dims, SEED)
     vh = int(np.prod(dims)) // 2
     ctx = wd.Context(local)
     lat = ctx.lattice(dims, gauge)
-    fin, fout = lat.field(src), lat.field()
+    fin, fout = lat.field(src, prec=prec), lat.field(prec=prec)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
 
     def barrier():
@@ -238,7 +243,7 @@ def run_ours(args) -> None:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_max = float(t.item())
-    value = world * BYTES_PER_SITE_F64 * vh / (t_max * 1e-3) / 1e9
+    value = world * bps * vh / (t_max * 1e-3) / 1e9
 
     # e2e through the reference-facing entry point, pinned host buffers
     e2e = None
@@ -265,11 +270,11 @@ def run_ours(args) -> None:
     if rank == 0:
         peak, peak_src = measured_peak_hbm()
         fp64_peak, fp32_peak = ctx.fma_peak()
-        achieved = BYTES_PER_SITE_F64 * vh / (ms * 1e-3) / 1e9
+        achieved = bps * vh / (ms * 1e-3) / 1e9
         gflops = FLOPS_PER_SITE * vh / (ms * 1e-3) / 1e9
         traffic = profiled_traffic(f"dslash_{args.prec}_32c64.md")
         line = {
-            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "metric": METRIC if args.prec == "f64" else METRIC.replace("FP64", args.prec.upper()), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.prec,
             "data": "synthetic (seeded SU(3) links eps=0.5, unit Gaussian source)",
@@ -305,7 +310,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--prec", choices=["f64", "df64"], default="f64")
+    ap.add_argument("--prec", choices=["f64", "df64", "f32", "f16"], default="f64",
+                    help="storage/arithmetic of the timed kernel (e2e always uses the FP64 drop-in path)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--dims", type=int, nargs=4, default=list(DIMS),

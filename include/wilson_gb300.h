@@ -79,6 +79,11 @@ int64_t wd_lattice_volume(const wd_lattice *lat);
 
 /* ---- fermion fields (replaces lattice_fermion, include/lattice_fermion.h:12-32) ---- */
 wd_status wd_field_create(wd_context *ctx, const wd_lattice *lat, wd_field **f);
+/* A field stored in another format (WD_PREC_DF64 float pairs, WD_PREC_F32, or
+ * WD_PREC_F16 with per-site scale); upload/download convert from/to FP64.
+ * Operators on such fields run in the arithmetic of their storage. */
+wd_status wd_field_create_prec(wd_context *ctx, const wd_lattice *lat, wd_precision prec, wd_field **f);
+wd_precision wd_field_precision(const wd_field *f);
 void wd_field_destroy(wd_field *f);
 /* host: V*12 complex doubles in the reference layout */
 wd_status wd_field_upload(wd_context *ctx, wd_field *f, const double *host);
@@ -124,6 +129,8 @@ typedef struct wd_solver_params {
     wd_precision prec;   /* arithmetic of the inner hopping kernel; FP64/DF64 or mixed F32/F16 */
     double delta;        /* reliable-update threshold for mixed precision (0 -> 0.1) */
     int use_initial_guess; /* CG_EO: 1 = start from dest, 0 = start from zero */
+    wd_precision prec_reliable; /* mixed precision: arithmetic of the reliable updates and of
+                                   the solution accumulation, WD_PREC_F64 or WD_PREC_DF64 */
 } wd_solver_params;
 
 typedef struct wd_solver_stats {

@@ -196,20 +196,32 @@ extern "C" void wd_lattice_destroy(wd_lattice *lat)
 extern "C" int64_t wd_lattice_volume(const wd_lattice *lat) { return lat ? lat->volume : 0; }
 
 // ------------------------------------------------------------------ fields
-extern "C" wd_status wd_field_create(wd_context *ctx, const wd_lattice *lat, wd_field **out)
+static size_t field_bytes(const wd_lattice *lat, wd_precision prec)
+{
+    size_t b = (size_t)lat->volume * 12 * wd_entry_bytes(prec);
+    if (prec == WD_PREC_F16) b += (size_t)lat->volume * sizeof(float);
+    return b;
+}
+
+extern "C" wd_status wd_field_create_prec(wd_context *ctx, const wd_lattice *lat, wd_precision prec, wd_field **out)
 {
     if (!ctx || !lat || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if (prec < WD_PREC_F64 || prec > WD_PREC_F16) return wd_fail(ctx, WD_ERR_BAD_ARG, "unknown precision");
     *out = nullptr;
     wd_field *f = new wd_field();
     f->lat = lat;
-    cudaError_t e = cudaMalloc(&f->d, (size_t)lat->volume * 12 * sizeof(double2));
+    f->storage = prec;
+    const size_t bytes = field_bytes(lat, prec);
+    cudaError_t e = cudaMalloc(&f->data, bytes);
     if (e != cudaSuccess) {
         delete f;
         return wd_cuda_check(ctx, e, "cudaMalloc(field)");
     }
-    e = cudaMemsetAsync(f->d, 0, (size_t)lat->volume * 12 * sizeof(double2), ctx->stream);
+    if (prec == WD_PREC_F64) f->d = (double2 *)f->data;
+    if (prec == WD_PREC_F16) f->scale = (float *)((char *)f->data + (size_t)lat->volume * 12 * wd_entry_bytes(prec));
+    e = cudaMemsetAsync(f->data, 0, bytes, ctx->stream);
     if (e != cudaSuccess) {
-        cudaFree(f->d);
+        cudaFree(f->data);
         delete f;
         return wd_cuda_check(ctx, e, "cudaMemsetAsync(field)");
     }
@@ -217,13 +229,21 @@ extern "C" wd_status wd_field_create(wd_context *ctx, const wd_lattice *lat, wd_
     return WD_OK;
 }
 
+extern "C" wd_status wd_field_create(wd_context *ctx, const wd_lattice *lat, wd_field **out)
+{
+    return wd_field_create_prec(ctx, lat, WD_PREC_F64, out);
+}
+
+extern "C" wd_precision wd_field_precision(const wd_field *f) { return f ? f->storage : WD_PREC_F64; }
+
 extern "C" void wd_field_destroy(wd_field *f)
 {
     if (!f) return;
-    cudaFree(f->d);  // cudaFree waits for work in flight on the device
+    cudaFree(f->data);  // cudaFree waits for work in flight on the device
     delete f;
 }
 
+// FP64 SoA staging <-> any storage (F16 goes through the FP32 layout kernel of wd_mixed.cu)
 extern "C" wd_status wd_field_upload(wd_context *ctx, wd_field *f, const double *host)
 {
     if (!ctx || !f || !host) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
@@ -231,7 +251,10 @@ extern "C" wd_status wd_field_upload(wd_context *ctx, wd_field *f, const double 
     wd_status st = ensure_staging(ctx, bytes);
     if (st != WD_OK) return st;
     WD_CUDA(ctx, cudaMemcpyAsync(ctx->staging, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    st = wd_spinor_ref_to_soa(ctx, f->lat->g, (const double2 *)ctx->staging, f->d);
+    if (f->storage == WD_PREC_F16)
+        st = wd_spinor_ref_to_h16(ctx, f->lat->g, (const double2 *)ctx->staging, wd_whole(f));
+    else
+        st = wd_spinor_ref_to_soa(ctx, f->lat->g, (const double2 *)ctx->staging, wd_whole(f));
     if (st != WD_OK) return st;
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return WD_OK;
@@ -243,7 +266,10 @@ extern "C" wd_status wd_field_download(wd_context *ctx, const wd_field *f, doubl
     const size_t bytes = (size_t)f->lat->volume * 12 * sizeof(double2);
     wd_status st = ensure_staging(ctx, bytes);
     if (st != WD_OK) return st;
-    st = wd_spinor_soa_to_ref(ctx, f->lat->g, f->d, (double2 *)ctx->staging);
+    if (f->storage == WD_PREC_F16)
+        st = wd_spinor_h16_to_ref(ctx, f->lat->g, wd_whole(f), (double2 *)ctx->staging);
+    else
+        st = wd_spinor_soa_to_ref(ctx, f->lat->g, wd_whole(f), (double2 *)ctx->staging);
     if (st != WD_OK) return st;
     WD_CUDA(ctx, cudaMemcpyAsync(host, ctx->staging, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -253,16 +279,17 @@ extern "C" wd_status wd_field_download(wd_context *ctx, const wd_field *f, doubl
 extern "C" wd_status wd_field_zero(wd_context *ctx, wd_field *f)
 {
     if (!ctx || !f) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
-    WD_CUDA(ctx, cudaMemsetAsync(f->d, 0, (size_t)f->lat->volume * 12 * sizeof(double2), ctx->stream));
+    WD_CUDA(ctx, cudaMemsetAsync(f->data, 0, field_bytes(f->lat, f->storage), ctx->stream));
     return WD_OK;
 }
 
 extern "C" wd_status wd_field_copy(wd_context *ctx, wd_field *dst, const wd_field *src)
 {
     if (!ctx || !dst || !src) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
-    if (dst->lat->volume != src->lat->volume) return wd_fail(ctx, WD_ERR_BAD_ARG, "field size mismatch");
-    WD_CUDA(ctx, cudaMemcpyAsync(dst->d, src->d, (size_t)src->lat->volume * 12 * sizeof(double2),
-                                 cudaMemcpyDeviceToDevice, ctx->stream));
+    if (dst->lat->volume != src->lat->volume || dst->storage != src->storage)
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "field size or storage mismatch");
+    WD_CUDA(ctx, cudaMemcpyAsync(dst->data, src->data, field_bytes(src->lat, src->storage), cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
     return WD_OK;
 }
 
@@ -273,67 +300,111 @@ static wd_status check_fields(wd_context *ctx, const wd_lattice *lat, const wd_f
     if (a->lat->volume != lat->volume || b->lat->volume != lat->volume)
         return wd_fail(ctx, WD_ERR_BAD_ARG, "field does not belong to this lattice size");
     if (a == b) return wd_fail(ctx, WD_ERR_BAD_ARG, "input and output must be different fields");
+    if (a->storage != b->storage) return wd_fail(ctx, WD_ERR_BAD_ARG, "input and output storage differ");
     return WD_OK;
 }
 
-// out_cb = alpha * D_{cb,1-cb} in_{1-cb} + beta * x_cb, dispatched on precision.
-wd_status wd_hop(wd_context *ctx, const wd_lattice *lat, const double2 *in_block, double2 *out_block,
-                 const double2 *x_block, int cb, int dag, double alpha, double beta, wd_precision prec)
+// out_cb = alpha * D_{cb,1-cb} in_{1-cb} + beta * x_cb on blocks of one storage format.
+wd_status wd_hop_v(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
+                   double alpha, double beta)
 {
-    switch (prec) {
-    case WD_PREC_F64: return wd_hop_f64(ctx, lat, in_block, out_block, x_block, cb, dag, alpha, beta);
-    default: return wd_fail(ctx, WD_ERR_BAD_ARG, "precision not available for FP64 fields");
+    if (in.prec != out.prec || (x && x->prec != in.prec))
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "hopping term operands have different storage");
+    switch (in.prec) {
+    case WD_PREC_F64:
+        return wd_hop_f64(ctx, lat, (const double2 *)in.p, (double2 *)out.p, x ? (const double2 *)x->p : nullptr, cb,
+                          dag, alpha, beta);
+    case WD_PREC_DF64:
+        return wd_hop_df(ctx, lat, (const float4 *)in.p, (float4 *)out.p, x ? (const float4 *)x->p : nullptr, cb, dag,
+                         alpha, beta);
+    case WD_PREC_F32: return wd_hop_f32(ctx, lat, in, out, x, cb, dag, alpha, beta);
+    case WD_PREC_F16: return wd_hop_f16(ctx, lat, in, out, x, cb, dag, alpha, beta);
     }
+    return wd_fail(ctx, WD_ERR_BAD_ARG, "unknown precision");
 }
 
-extern "C" wd_status wd_dslash_offd(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
-                                    wd_field *out, int dag, int cb, wd_precision prec)
+// Runs `op` on df copies when an FP64 field is asked for double-float
+// arithmetic; otherwise the arithmetic must match the storage.
+template <class Op>
+static wd_status with_arith(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                            wd_precision prec, bool out_needs_init, Op op)
+{
+    if (prec == in->storage) return op(in, out);
+    if (!(in->storage == WD_PREC_F64 && prec == WD_PREC_DF64))
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "arithmetic precision does not match the fields' storage");
+    wd_field *ti = nullptr, *to = nullptr;
+    wd_status st = wd_field_create_prec(ctx, lat, WD_PREC_DF64, &ti);
+    if (st == WD_OK) st = wd_field_create_prec(ctx, lat, WD_PREC_DF64, &to);
+    const int64_t n = lat->volume * 12;
+    if (st == WD_OK) st = wd_convert_f64_to_df(ctx, in->d, (float4 *)ti->data, n);
+    if (st == WD_OK && out_needs_init) st = wd_convert_f64_to_df(ctx, out->d, (float4 *)to->data, n);
+    if (st == WD_OK) st = op(ti, to);
+    if (st == WD_OK) st = wd_convert_df_to_f64(ctx, (const float4 *)to->data, out->d, n);
+    wd_field_destroy(ti);
+    wd_field_destroy(to);
+    return st;
+}
+
+extern "C" wd_status wd_dslash_offd(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                                    int dag, int cb, wd_precision prec)
 {
     wd_status st = check_fields(ctx, lat, in, out);
     if (st != WD_OK) return st;
     if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
-    const int Vh = lat->g.Vh;
-    const size_t blk = (size_t)12 * Vh;
-    // the reference zeroes the whole destination (src/dslash_new.cpp:1398)
-    WD_CUDA(ctx, cudaMemsetAsync(out->d + (1 - cb) * blk, 0, blk * sizeof(double2), ctx->stream));
-    return wd_hop(ctx, lat, in->d + (1 - cb) * blk, out->d + cb * blk, nullptr, cb, dag, -0.5, 0.0, prec);
+    return with_arith(ctx, lat, in, out, prec, false, [&](const wd_field *i, wd_field *o) -> wd_status {
+        // the reference zeroes the whole destination (src/dslash_new.cpp:1398)
+        wd_status s = wd_v_zero(ctx, wd_block(o, 1 - cb), (int64_t)12 * lat->g.Vh);
+        if (s != WD_OK) return s;
+        return wd_hop_v(ctx, lat, wd_block(i, 1 - cb), wd_block(o, cb), nullptr, cb, dag, -0.5, 0.0);
+    });
 }
 
-extern "C" wd_status wd_dslash_eo(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
-                                  wd_field *out, int dag, int cb, wd_precision prec)
+extern "C" wd_status wd_dslash_eo(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                                  int dag, int cb, wd_precision prec)
 {
     wd_status st = check_fields(ctx, lat, in, out);
     if (st != WD_OK) return st;
     if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
-    const size_t blk = (size_t)12 * lat->g.Vh;
-    return wd_hop(ctx, lat, in->d + (1 - cb) * blk, out->d + cb * blk, nullptr, cb, dag, -0.5, 0.0, prec);
+    return with_arith(ctx, lat, in, out, prec, true, [&](const wd_field *i, wd_field *o) -> wd_status {
+        return wd_hop_v(ctx, lat, wd_block(i, 1 - cb), wd_block(o, cb), nullptr, cb, dag, -0.5, 0.0);
+    });
 }
 
-extern "C" wd_status wd_dslash_eeoo(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
-                                    wd_field *out, double mass)
-{
-    if (!ctx || !lat || !in || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
-    return wd_blas_scale(ctx, 4.0 + mass, in->d, out->d, lat->volume * 12);
-}
-
-extern "C" wd_status wd_dslash_full(wd_context *ctx, const wd_lattice *lat, const wd_field *in,
-                                    wd_field *out, double mass, int dag, wd_precision prec)
+extern "C" wd_status wd_dslash_eeoo(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                                    double mass)
 {
     wd_status st = check_fields(ctx, lat, in, out);
     if (st != WD_OK) return st;
-    const size_t blk = (size_t)12 * lat->g.Vh;
-    const double a = 4.0 + mass;
-    for (int cb = 0; cb < 2; ++cb) {
-        st = wd_hop(ctx, lat, in->d + (1 - cb) * blk, out->d + cb * blk, in->d + cb * blk, cb, dag, -0.5, a, prec);
+    const int64_t n = lat->volume * 12;
+    if (in->storage == WD_PREC_F64) return wd_blas_scale(ctx, 4.0 + mass, in->d, out->d, n);
+    if (in->storage == WD_PREC_DF64) {
+        st = wd_v_zero(ctx, wd_whole(out), n);
         if (st != WD_OK) return st;
+        return wd_v_axpby(ctx, make_double2(4.0 + mass, 0.0), wd_whole(in), make_double2(0.0, 0.0), wd_whole(out), n);
     }
-    return WD_OK;
+    return wd_fail(ctx, WD_ERR_BAD_ARG, "DslashEEOO needs FP64 or double-float fields");
+}
+
+extern "C" wd_status wd_dslash_full(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out,
+                                    double mass, int dag, wd_precision prec)
+{
+    wd_status st = check_fields(ctx, lat, in, out);
+    if (st != WD_OK) return st;
+    const double a = 4.0 + mass;
+    return with_arith(ctx, lat, in, out, prec, false, [&](const wd_field *i, wd_field *o) -> wd_status {
+        for (int cb = 0; cb < 2; ++cb) {
+            const WdVec x = wd_block(i, cb);
+            wd_status s = wd_hop_v(ctx, lat, wd_block(i, 1 - cb), wd_block(o, cb), &x, cb, dag, -0.5, a);
+            if (s != WD_OK) return s;
+        }
+        return WD_OK;
+    });
 }
 
 extern "C" wd_status wd_norm2(wd_context *ctx, const wd_field *a, double *out)
 {
     if (!ctx || !a || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
-    wd_status st = wd_red_norm2(ctx, a->d, a->lat->volume * 12, 0);
+    wd_status st = wd_v_norm2(ctx, wd_whole(a), a->lat->volume * 12, 0);
     if (st != WD_OK) return st;
     double2 r;
     st = wd_red_fetch(ctx, 1, &r);
@@ -345,7 +416,7 @@ extern "C" wd_status wd_dot(wd_context *ctx, const wd_field *a, const wd_field *
 {
     if (!ctx || !a || !b || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
     if (a->lat->volume != b->lat->volume) return wd_fail(ctx, WD_ERR_BAD_ARG, "field size mismatch");
-    wd_status st = wd_red_dot(ctx, a->d, b->d, a->lat->volume * 12, 0);
+    wd_status st = wd_v_dot(ctx, wd_whole(a), wd_whole(b), a->lat->volume * 12, 0);
     if (st != WD_OK) return st;
     double2 r;
     st = wd_red_fetch(ctx, 1, &r);

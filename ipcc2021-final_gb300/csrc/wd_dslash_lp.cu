@@ -1,0 +1,238 @@
+// wd_dslash_lp.cu -- FP32 and FP16 hopping kernels (12-real links, FP32
+// arithmetic) and the conversions between FP64 and the low-precision
+// storage formats of wd_lp.cuh.
+//
+// Compulsory bytes per output site: FP32 8*48 + 96 + 96 = 576 B;
+// FP16 8*24 + 52 + 52 = 296 B (+ one spinor read when the epilogue uses x).
+// Both are HBM-bound: 1320 flop/site (+ 8 x 66 for the row-2 rebuild) is far
+// below the FP32 ridge.
+#include "wd_hop.cuh"
+#include "wd_lp.cuh"
+#include "wd_kernels.h"
+
+namespace {
+
+template <class Sp, class Lk>
+struct HopLP {
+    using C = float2;
+    static constexpr int kThreads = 128;
+    WdGeom g;
+    int cb;
+    Sp in, out, x;
+    Lk link;
+    bool has_x;
+    float alpha, beta;
+
+    __device__ __forceinline__ void load_in(int s, C *v) const { in.load(s, v); }
+    __device__ __forceinline__ void load_link(int mu, int par, int s, C *U) const { link.load(mu, par, s, U); }
+    __device__ __forceinline__ void epilogue(int s, const C *acc) const
+    {
+        C r[12];
+        if (has_x) {
+            C xv[12];
+            x.load(s, xv);
+#pragma unroll
+            for (int c = 0; c < 12; ++c) r[c] = c_axpby(alpha, acc[c], beta, xv[c]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 12; ++c) r[c] = c_scale(acc[c], alpha);
+        }
+        out.store(s, r);
+    }
+};
+
+// links: FP64 planes [mu][par][9][Vh] -> rows 0,1 in FP32 / FP16
+__global__ void k_gauge_f32(const double2 *__restrict__ g, float4 *__restrict__ out, int Vh)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mp = blockIdx.y;  // mu*2 + par
+    if (s >= Vh) return;
+    const double2 *b = g + (size_t)mp * 9 * Vh + s;
+    float4 *o = out + (size_t)mp * 3 * Vh + s;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const double2 u0 = b[(size_t)(2 * j) * Vh], u1 = b[(size_t)(2 * j + 1) * Vh];
+        o[(size_t)j * Vh] = make_float4((float)u0.x, (float)u0.y, (float)u1.x, (float)u1.y);
+    }
+}
+
+__global__ void k_gauge_f16(const double2 *__restrict__ g, uint4 *__restrict__ a, uint2 *__restrict__ bb, int Vh)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mp = blockIdx.y;
+    if (s >= Vh) return;
+    const double2 *b = g + (size_t)mp * 9 * Vh + s;
+    float2 u[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        const double2 v = b[(size_t)k * Vh];
+        u[k] = make_float2((float)v.x, (float)v.y);
+    }
+    a[(size_t)mp * Vh + s] = pack4(u);
+    __half2 h4 = f2h(u[4]), h5 = f2h(u[5]);
+    bb[(size_t)mp * Vh + s] = make_uint2(*reinterpret_cast<unsigned *>(&h4), *reinterpret_cast<unsigned *>(&h5));
+}
+
+// FP64 SoA block [12][Vh] <-> low-precision block, one thread per site
+template <class Sp>
+__global__ void k_from_f64(const double2 *__restrict__ in, Sp out, int Vh)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= Vh) return;
+    float2 v[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) {
+        const double2 d = in[(size_t)c * Vh + s];
+        v[c] = make_float2((float)d.x, (float)d.y);
+    }
+    out.store(s, v);
+}
+
+template <class Sp>
+__global__ void k_to_f64(Sp in, double2 *__restrict__ out, int Vh, int accumulate)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= Vh) return;
+    float2 v[12];
+    in.load(s, v);
+#pragma unroll
+    for (int c = 0; c < 12; ++c) {
+        double2 d = make_double2(v[c].x, v[c].y);
+        if (accumulate) {
+            const double2 o = out[(size_t)c * Vh + s];
+            d.x += o.x;
+            d.y += o.y;
+        }
+        out[(size_t)c * Vh + s] = d;
+    }
+}
+
+// reference AoS (both parities) <-> FP16 field
+__global__ void k_aos_to_h16(const double2 *__restrict__ aos, SpF16 out, int Vh)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= Vh) return;
+    float2 v[12];
+#pragma unroll
+    for (int c = 0; c < 12; ++c) {
+        const double2 d = aos[(size_t)s * 12 + c];
+        v[c] = make_float2((float)d.x, (float)d.y);
+    }
+    out.store(s, v);
+}
+
+__global__ void k_h16_to_aos(SpF16 in, double2 *__restrict__ aos, int Vh)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= Vh) return;
+    float2 v[12];
+    in.load(s, v);
+#pragma unroll
+    for (int c = 0; c < 12; ++c) aos[(size_t)s * 12 + c] = make_double2(v[c].x, v[c].y);
+}
+
+inline int site_blocks(int Vh) { return (Vh + 127) / 128; }
+
+template <class P>
+wd_status launch_hop(wd_context *ctx, const P &p, int dag)
+{
+    const int blocks = (p.g.Vh + P::kThreads - 1) / P::kThreads;
+    if (dag) wd_hop_kernel<true><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+    else wd_hop_kernel<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}
+
+}  // namespace
+
+wd_status wd_lattice_gauge_lp(wd_context *ctx, const wd_lattice *lat_c, wd_precision prec)
+{
+    wd_lattice *lat = const_cast<wd_lattice *>(lat_c);
+    const int Vh = lat->g.Vh;
+    dim3 grid((Vh + 127) / 128, 8);
+    if (prec == WD_PREC_F32) {
+        if (lat->gauge_f32) return WD_OK;
+        WD_CUDA(ctx, cudaMalloc(&lat->gauge_f32, (size_t)8 * 3 * Vh * sizeof(float4)));
+        k_gauge_f32<<<grid, 128, 0, ctx->stream>>>(lat->gauge, (float4 *)lat->gauge_f32, Vh);
+    } else {
+        if (lat->gauge_h12) return WD_OK;
+        WD_CUDA(ctx, cudaMalloc(&lat->gauge_h12, (size_t)8 * Vh * (sizeof(uint4) + sizeof(uint2))));
+        uint4 *a = (uint4 *)lat->gauge_h12;
+        k_gauge_f16<<<grid, 128, 0, ctx->stream>>>(lat->gauge, a, (uint2 *)(a + (size_t)8 * Vh), Vh);
+    }
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}
+
+wd_status wd_hop_f32(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
+                     double alpha, double beta)
+{
+    wd_status st = wd_lattice_gauge_lp(ctx, lat, WD_PREC_F32);
+    if (st != WD_OK) return st;
+    HopLP<SpF32, LinkF32> p;
+    p.g = lat->g;
+    p.cb = cb;
+    p.in = sp_f32(in, lat->g.Vh);
+    p.out = sp_f32(out, lat->g.Vh);
+    p.has_x = x != nullptr;
+    p.x = x ? sp_f32(*x, lat->g.Vh) : p.out;
+    p.link = LinkF32{(const float4 *)lat->gauge_f32, lat->g.Vh};
+    p.alpha = (float)alpha;
+    p.beta = (float)beta;
+    return launch_hop(ctx, p, dag);
+}
+
+wd_status wd_hop_f16(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
+                     double alpha, double beta)
+{
+    wd_status st = wd_lattice_gauge_lp(ctx, lat, WD_PREC_F16);
+    if (st != WD_OK) return st;
+    HopLP<SpF16, LinkF16> p;
+    p.g = lat->g;
+    p.cb = cb;
+    p.in = sp_f16(in, lat->g.Vh);
+    p.out = sp_f16(out, lat->g.Vh);
+    p.has_x = x != nullptr;
+    p.x = x ? sp_f16(*x, lat->g.Vh) : p.out;
+    const uint4 *a = (const uint4 *)lat->gauge_h12;
+    p.link = LinkF16{a, (const uint2 *)(a + (size_t)8 * lat->g.Vh), lat->g.Vh};
+    p.alpha = (float)alpha;
+    p.beta = (float)beta;
+    return launch_hop(ctx, p, dag);
+}
+
+wd_status wd_lp_from_f64(wd_context *ctx, int Vh, const double2 *in, WdVec out)
+{
+    if (out.prec == WD_PREC_F32) k_from_f64<<<site_blocks(Vh), 128, 0, ctx->stream>>>(in, sp_f32(out, Vh), Vh);
+    else k_from_f64<<<site_blocks(Vh), 128, 0, ctx->stream>>>(in, sp_f16(out, Vh), Vh);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}
+
+wd_status wd_lp_to_f64(wd_context *ctx, int Vh, WdVec in, double2 *out, int accumulate)
+{
+    if (in.prec == WD_PREC_F32) k_to_f64<<<site_blocks(Vh), 128, 0, ctx->stream>>>(sp_f32(in, Vh), out, Vh, accumulate);
+    else k_to_f64<<<site_blocks(Vh), 128, 0, ctx->stream>>>(sp_f16(in, Vh), out, Vh, accumulate);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}
+
+wd_status wd_spinor_ref_to_h16(wd_context *ctx, const WdGeom &g, const double2 *ref, WdVec f)
+{
+    for (int par = 0; par < 2; ++par) {
+        const WdVec b = wd_offset(f, (int64_t)par * 12 * g.Vh, (int64_t)par * g.Vh);
+        k_aos_to_h16<<<site_blocks(g.Vh), 128, 0, ctx->stream>>>(ref + (size_t)par * 12 * g.Vh, sp_f16(b, g.Vh), g.Vh);
+        WD_LAUNCHED(ctx);
+    }
+    return WD_OK;
+}
+
+wd_status wd_spinor_h16_to_ref(wd_context *ctx, const WdGeom &g, WdVec f, double2 *ref)
+{
+    for (int par = 0; par < 2; ++par) {
+        const WdVec b = wd_offset(f, (int64_t)par * 12 * g.Vh, (int64_t)par * g.Vh);
+        k_h16_to_aos<<<site_blocks(g.Vh), 128, 0, ctx->stream>>>(sp_f16(b, g.Vh), ref + (size_t)par * 12 * g.Vh, g.Vh);
+        WD_LAUNCHED(ctx);
+    }
+    return WD_OK;
+}

@@ -46,14 +46,60 @@ struct wd_lattice {
     int64_t volume = 0;
     double2 *gauge = nullptr;     // FP64 [mu][parity][9][Vh]
     float4 *gauge_df = nullptr;   // double-float copy, same shape (lazily built)
-    float2 *gauge_f32 = nullptr;  // FP32 18-real [mu][parity][9][Vh] (lazily built)
-    void *gauge_h12 = nullptr;    // FP16 12-real links (lazily built)
+    void *gauge_f32 = nullptr;    // FP32 12-real links [mu][parity][3][Vh] float4 (lazily built)
+    void *gauge_h12 = nullptr;    // FP16 12-real links: uint4 [8][Vh] then uint2 [8][Vh] (lazily built)
 };
 
 struct wd_field {
     const wd_lattice *lat = nullptr;
-    double2 *d = nullptr;  // [parity][12][Vh]
+    wd_precision storage = WD_PREC_F64;
+    void *data = nullptr;     // [parity][12][Vh] entries of the storage type
+    float *scale = nullptr;   // FP16 storage: [parity][Vh] per-site scales (inside data)
+    double2 *d = nullptr;     // == data for FP64 storage, else null
 };
+
+// A typed view of a spinor array (one parity block or a whole field).
+struct WdVec {
+    void *p = nullptr;
+    float *scale = nullptr;  // FP16 only
+    wd_precision prec = WD_PREC_F64;
+};
+
+// bytes of one complex entry in each storage format (FP16: half2 + scale per 12 entries)
+inline size_t wd_entry_bytes(wd_precision p)
+{
+    switch (p) {
+    case WD_PREC_F64: return 16;
+    case WD_PREC_DF64: return 16;
+    case WD_PREC_F32: return 8;
+    default: return 4;
+    }
+}
+
+// view of parity block `par` (0/1) of a field
+inline WdVec wd_block(const wd_field *f, int par)
+{
+    WdVec v;
+    v.prec = f->storage;
+    const size_t blk = (size_t)12 * f->lat->g.Vh;
+    v.p = (char *)f->data + par * blk * wd_entry_bytes(f->storage);
+    if (f->scale) v.scale = f->scale + (size_t)par * f->lat->g.Vh;
+    return v;
+}
+inline WdVec wd_whole(const wd_field *f)
+{
+    WdVec v;
+    v.prec = f->storage;
+    v.p = f->data;
+    v.scale = f->scale;
+    return v;
+}
+inline WdVec wd_offset(WdVec v, int64_t entries, int64_t sites)
+{
+    v.p = (char *)v.p + entries * (int64_t)wd_entry_bytes(v.prec);
+    if (v.scale) v.scale += sites;
+    return v;
+}
 
 // Error plumbing: record text on the context and return a status.
 wd_status wd_fail(wd_context *ctx, wd_status s, const std::string &msg);

@@ -15,9 +15,9 @@ wd_status wd_hop_f64(wd_context *ctx, const wd_lattice *lat, const double2 *in_b
                      double beta);
 
 // ---- layout conversion (reference AoS <-> device SoA), on device buffers
-// spinor: ref[(p*Vh + s)*12 + c]  <->  soa[(p*12 + c)*Vh + s]
-wd_status wd_spinor_ref_to_soa(wd_context *ctx, const WdGeom &g, const double2 *ref, double2 *soa);
-wd_status wd_spinor_soa_to_ref(wd_context *ctx, const WdGeom &g, const double2 *soa, double2 *ref);
+// spinor: ref[(p*Vh + s)*12 + c]  <->  soa[(p*12 + c)*Vh + s] in the vector's storage format
+wd_status wd_spinor_ref_to_soa(wd_context *ctx, const WdGeom &g, const double2 *ref, WdVec soa);
+wd_status wd_spinor_soa_to_ref(wd_context *ctx, const WdGeom &g, WdVec soa, double2 *ref);
 // gauge, one direction: ref[(p*Vh + s)*9 + k]  ->  soa[((mu*2 + p)*9 + k)*Vh + s]
 wd_status wd_gauge_ref_to_soa(wd_context *ctx, const WdGeom &g, int mu, const double2 *ref,
                               double2 *soa);
@@ -26,6 +26,8 @@ wd_status wd_gauge_ref_to_soa(wd_context *ctx, const WdGeom &g, int mu, const do
 // results of reductions are written to ctx->red_partial[WD_RED_BLOCKS + slot]
 wd_status wd_red_norm2(wd_context *ctx, const double2 *a, int64_t n, int slot);
 wd_status wd_red_dot(wd_context *ctx, const double2 *a, const double2 *b, int64_t n, int slot);
+// fold the WD_RED_BLOCKS partials written by a reduction kernel into result slot `slot`
+wd_status wd_red_finish(wd_context *ctx, int slot);
 // copy result slots [0, nslots) to the host (synchronises the stream)
 wd_status wd_red_fetch(wd_context *ctx, int nslots, double2 *host);
 // y = a*x + b*y   (a, b complex)
@@ -39,3 +41,35 @@ wd_status wd_blas_cg_update(wd_context *ctx, double2 alpha, const double2 *p, co
                             double2 *x, double2 *r, int64_t n, int slot);
 // y = a*x (real a)
 wd_status wd_blas_scale(wd_context *ctx, double a, const double2 *x, double2 *y, int64_t n);
+
+// ---- double-float (df64) storage: float4 {re.h, re.l, im.h, im.l} per complex
+wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_block, float4 *out_block,
+                    const float4 *x_block, int cb, int dag, double alpha, double beta);
+wd_status wd_convert_f64_to_df(wd_context *ctx, const double2 *in, float4 *out, int64_t n);
+wd_status wd_convert_df_to_f64(wd_context *ctx, const float4 *in, double2 *out, int64_t n);
+wd_status wd_lattice_gauge_df(wd_context *ctx, const wd_lattice *lat);
+
+// ---- BLAS-1 dispatched on the storage of the vectors (FP64 or double-float);
+// n counts complex entries.  Reductions land in result slot `slot`.
+wd_status wd_v_norm2(wd_context *ctx, WdVec a, int64_t n, int slot);
+wd_status wd_v_dot(wd_context *ctx, WdVec a, WdVec b, int64_t n, int slot);
+wd_status wd_v_axpby(wd_context *ctx, double2 a, WdVec x, double2 b, WdVec y, int64_t n);
+wd_status wd_v_xpayz(wd_context *ctx, WdVec x, double2 a, WdVec y, WdVec z, int64_t n);
+wd_status wd_v_cg_update(wd_context *ctx, double2 alpha, WdVec p, WdVec q, WdVec x, WdVec r, int64_t n, int slot);
+wd_status wd_v_copy(wd_context *ctx, WdVec dst, WdVec src, int64_t n);
+wd_status wd_v_zero(wd_context *ctx, WdVec v, int64_t n);
+
+// ---- FP32 / FP16 storage (wd_lp.cuh) with 12-real links
+wd_status wd_lattice_gauge_lp(wd_context *ctx, const wd_lattice *lat, wd_precision prec);
+wd_status wd_hop_f32(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
+                     double alpha, double beta);
+wd_status wd_hop_f16(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
+                     double alpha, double beta);
+// FP64 block [12][Vh] <-> low-precision block; accumulate != 0 adds into out
+wd_status wd_lp_from_f64(wd_context *ctx, int Vh, const double2 *in, WdVec out);
+wd_status wd_lp_to_f64(wd_context *ctx, int Vh, WdVec in, double2 *out, int accumulate);
+wd_status wd_spinor_ref_to_h16(wd_context *ctx, const WdGeom &g, const double2 *ref, WdVec f);
+wd_status wd_spinor_h16_to_ref(wd_context *ctx, const WdGeom &g, WdVec f, double2 *ref);
+// out_cb = alpha * D_{cb,1-cb} in_{1-cb} + beta * x_cb, dispatched on the storage
+wd_status wd_hop_v(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
+                   double alpha, double beta);

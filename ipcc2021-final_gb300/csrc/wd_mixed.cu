@@ -1,9 +1,312 @@
-// wd_mixed.cu -- mixed-precision even-odd CG with FP64 reliable updates.
-#include "wd_kernels.h"
+// wd_mixed.cu -- mixed-precision even-odd CG with reliable updates.
+//
+// The CG on Mhat^dag Mhat x_e = Mhat^dag bhat_e (Mhat = a - D_eo D_oe/(4a))
+// iterates in low precision: search direction and operator outputs in the
+// kernel storage (FP32, or FP16 with per-site scale; 12-real links), the
+// iterated residual r_s and the solution increment x_s in FP32, with
+// per-site double-float partial sums reduced in FP64.  Whenever the
+// low-precision residual has dropped by delta (default 0.1) since the last
+// update, or has reached the estimated target, a reliable update
+// (Sleijpen & van der Vorst) runs in high precision (FP64, or double-float
+// when prec_reliable = WD_PREC_DF64):
+//   x_e += x_s;  s = bhat - Mhat x_e;  r = Mhat^dag s;  r_s <- r;  x_s <- 0
+// |s| is the true residual |b - M x| of the full system, so convergence is
+// decided on the recomputed high-precision residual, never on the iterated one.
+#include <chrono>
+#include <cmath>
+#include "wd_df.cuh"
+#include "wd_lp.cuh"
+#include "wd_reduce.cuh"
 #include "wd_solver.h"
 
-wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *, const double2 *, double2 *,
-                               const wd_solver_params *, wd_solver_stats *)
+namespace {
+
+// high-precision (FP64 or double-float) block access in FP64 registers
+struct HF64 {
+    double2 *p;
+    int Vh;
+    __device__ double2 load(int c, int s) const { return p[(size_t)c * Vh + s]; }
+    __device__ void store(int c, int s, double2 v) const { p[(size_t)c * Vh + s] = v; }
+};
+struct HDF {
+    float4 *p;
+    int Vh;
+    __device__ double2 load(int c, int s) const { return df_unpack(p[(size_t)c * Vh + s]); }
+    __device__ void store(int c, int s, double2 v) const { p[(size_t)c * Vh + s] = df_pack(v); }
+};
+
+__device__ __forceinline__ dfr df_sq_acc(dfr acc, float2 v)
 {
-    return wd_fail(ctx, WD_ERR_BAD_ARG, "mixed-precision solver not built yet");
+    return df_madd(df_madd(acc, dfr{v.x, 0.f}, dfr{v.x, 0.f}), dfr{v.y, 0.f}, dfr{v.y, 0.f});
+}
+
+#define SITE_STRIDE(s, Vh) for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < (Vh); s += gridDim.x * blockDim.x)
+
+// x_s += alpha p; r_s -= alpha q; partial |r_s|^2
+template <class SpL>
+__global__ void __launch_bounds__(WD_RED_THREADS) k_mx_update(float alpha, SpL p, SpL q, SpF32 xs, SpF32 rs, int Vh,
+                                                              double2 *partial)
+{
+    dfr acc{0.f, 0.f};
+    SITE_STRIDE(s, Vh)
+    {
+        float2 pv[12], qv[12], xv[12], rv[12];
+        p.load(s, pv);
+        q.load(s, qv);
+        xs.load(s, xv);
+        rs.load(s, rv);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) {
+            xv[c] = make_float2(fmaf(alpha, pv[c].x, xv[c].x), fmaf(alpha, pv[c].y, xv[c].y));
+            rv[c] = make_float2(fmaf(-alpha, qv[c].x, rv[c].x), fmaf(-alpha, qv[c].y, rv[c].y));
+            acc = df_sq_acc(acc, rv[c]);
+        }
+        xs.store(s, xv);
+        rs.store(s, rv);
+    }
+    wd_block_partial(df_value(acc), 0.0, partial);
+}
+
+// p = r_s + beta p
+template <class SpL>
+__global__ void k_mx_xpay(SpF32 rs, float beta, SpL p, int Vh)
+{
+    SITE_STRIDE(s, Vh)
+    {
+        float2 rv[12], pv[12];
+        rs.load(s, rv);
+        p.load(s, pv);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) pv[c] = make_float2(fmaf(beta, pv[c].x, rv[c].x), fmaf(beta, pv[c].y, rv[c].y));
+        p.store(s, pv);
+    }
+}
+
+template <class SpL>
+__global__ void __launch_bounds__(WD_RED_THREADS) k_mx_norm2(SpL t, int Vh, double2 *partial)
+{
+    dfr acc{0.f, 0.f};
+    SITE_STRIDE(s, Vh)
+    {
+        float2 v[12];
+        t.load(s, v);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) acc = df_sq_acc(acc, v[c]);
+    }
+    wd_block_partial(df_value(acc), 0.0, partial);
+}
+
+// high precision -> low precision (two outputs: FP32 r_s and kernel-storage p)
+template <class H, class SpL>
+__global__ void k_mx_from_h(H in, SpF32 a, SpL b, int Vh)
+{
+    SITE_STRIDE(s, Vh)
+    {
+        float2 v[12];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) {
+            const double2 d = in.load(c, s);
+            v[c] = make_float2((float)d.x, (float)d.y);
+        }
+        a.store(s, v);
+        b.store(s, v);
+    }
+}
+
+// x_H += x_s; x_s = 0
+template <class H>
+__global__ void k_mx_accum(SpF32 xs, H x, int Vh)
+{
+    SITE_STRIDE(s, Vh)
+    {
+        float2 v[12];
+        xs.load(s, v);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) {
+            double2 d = x.load(c, s);
+            d.x += (double)v[c].x;
+            d.y += (double)v[c].y;
+            x.store(c, s, d);
+            v[c] = make_float2(0.f, 0.f);
+        }
+        xs.store(s, v);
+    }
+}
+
+// Reduction kernels always run the fixed grid of WD_RED_BLOCKS blocks (idle
+// blocks write zero partials): wd_red_finish folds exactly that many.
+inline int site_grid(int) { return WD_RED_BLOCKS; }
+
+// Typed launchers over (kernel storage L) x (high precision H)
+struct Mixed {
+    wd_context *ctx;
+    int Vh;
+    wd_precision L, H;
+
+    wd_status update(float alpha, WdVec p, WdVec q, WdVec xs, WdVec rs) const
+    {
+        double2 *part = (double2 *)ctx->red_partial;
+        if (L == WD_PREC_F32)
+            k_mx_update<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(alpha, sp_f32(p, Vh), sp_f32(q, Vh),
+                                                                          sp_f32(xs, Vh), sp_f32(rs, Vh), Vh, part);
+        else
+            k_mx_update<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(alpha, sp_f16(p, Vh), sp_f16(q, Vh),
+                                                                          sp_f32(xs, Vh), sp_f32(rs, Vh), Vh, part);
+        WD_LAUNCHED(ctx);
+        return wd_red_finish(ctx, 0);
+    }
+    wd_status xpay(WdVec rs, float beta, WdVec p) const
+    {
+        if (L == WD_PREC_F32) k_mx_xpay<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(rs, Vh), beta, sp_f32(p, Vh), Vh);
+        else k_mx_xpay<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(rs, Vh), beta, sp_f16(p, Vh), Vh);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    }
+    wd_status norm2(WdVec t) const
+    {
+        double2 *part = (double2 *)ctx->red_partial;
+        if (L == WD_PREC_F32) k_mx_norm2<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(t, Vh), Vh, part);
+        else k_mx_norm2<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f16(t, Vh), Vh, part);
+        WD_LAUNCHED(ctx);
+        return wd_red_finish(ctx, 0);
+    }
+    wd_status from_h(WdVec h, WdVec rs, WdVec p) const
+    {
+        const int g = site_grid(Vh);
+        if (H == WD_PREC_F64) {
+            const HF64 in{(double2 *)h.p, Vh};
+            if (L == WD_PREC_F32) k_mx_from_h<<<g, WD_RED_THREADS, 0, ctx->stream>>>(in, sp_f32(rs, Vh), sp_f32(p, Vh), Vh);
+            else k_mx_from_h<<<g, WD_RED_THREADS, 0, ctx->stream>>>(in, sp_f32(rs, Vh), sp_f16(p, Vh), Vh);
+        } else {
+            const HDF in{(float4 *)h.p, Vh};
+            if (L == WD_PREC_F32) k_mx_from_h<<<g, WD_RED_THREADS, 0, ctx->stream>>>(in, sp_f32(rs, Vh), sp_f32(p, Vh), Vh);
+            else k_mx_from_h<<<g, WD_RED_THREADS, 0, ctx->stream>>>(in, sp_f32(rs, Vh), sp_f16(p, Vh), Vh);
+        }
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    }
+    wd_status accum(WdVec xs, WdVec xh) const
+    {
+        const int g = site_grid(Vh);
+        if (H == WD_PREC_F64) k_mx_accum<<<g, WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(xs, Vh), HF64{(double2 *)xh.p, Vh}, Vh);
+        else k_mx_accum<<<g, WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(xs, Vh), HDF{(float4 *)xh.p, Vh}, Vh);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    }
+};
+
+inline WdVec par_half(WdVec v, int par, int Vh) { return wd_offset(v, (int64_t)par * 12 * Vh, (int64_t)par * Vh); }
+
+}  // namespace
+
+wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const double2 *src, double2 *x,
+                               const wd_solver_params *prm, wd_solver_stats *stats)
+{
+    const int Vh = lat->g.Vh;
+    const int64_t nh = (int64_t)12 * Vh, n = 2 * nh;
+    const double m = prm->mass, a = 4.0 + m;
+    const double delta = prm->delta > 0 && prm->delta < 1 ? prm->delta : 0.1;
+    const wd_precision H = prm->prec_reliable == WD_PREC_DF64 ? WD_PREC_DF64 : WD_PREC_F64;
+    const Mixed mx{ctx, Vh, prm->prec, H};
+    wd_status st;
+
+    // high-precision vectors: full source and solution, even-parity work blocks
+    WdVecBuf hs, hx, bhat, s_e, r_h, t_h, tmp_oh;
+    WdVecBuf p, t, q, tmp_ol, rs, xs;
+    WdVecBuf *hbufs[] = {&bhat, &s_e, &r_h, &t_h, &tmp_oh};
+    for (WdVecBuf *b : hbufs)
+        if ((st = wd_vec_alloc(ctx, *b, H, nh)) != WD_OK) return st;
+    WdVecBuf *lbufs[] = {&p, &t, &q, &tmp_ol};
+    for (WdVecBuf *b : lbufs)
+        if ((st = wd_vec_alloc(ctx, *b, prm->prec, nh)) != WD_OK) return st;
+    if ((st = wd_vec_alloc(ctx, rs, WD_PREC_F32, nh)) != WD_OK) return st;
+    if ((st = wd_vec_alloc(ctx, xs, WD_PREC_F32, nh)) != WD_OK) return st;
+    WdVec vsrc{(void *)src}, vx{(void *)x};
+    if (H == WD_PREC_DF64) {
+        if ((st = wd_vec_alloc(ctx, hs, H, n)) != WD_OK) return st;
+        if ((st = wd_vec_alloc(ctx, hx, H, n)) != WD_OK) return st;
+        if ((st = wd_convert_f64_to_df(ctx, src, (float4 *)hs.v.p, n)) != WD_OK) return st;
+        if ((st = wd_convert_f64_to_df(ctx, x, (float4 *)hx.v.p, n)) != WD_OK) return st;
+        vsrc = hs.v;
+        vx = hx.v;
+    }
+    const WdVec b_e = par_half(vsrc, 0, Vh), b_o = par_half(vsrc, 1, Vh);
+    const WdVec x_e = par_half(vx, 0, Vh), x_o = par_half(vx, 1, Vh);
+
+    if ((st = wd_hop_v(ctx, lat, b_o, bhat.v, &b_e, 0, 0, 0.5 / a, 1.0)) != WD_OK) return st;
+    if (!prm->use_initial_guess && (st = wd_v_zero(ctx, x_e, nh)) != WD_OK) return st;
+    if ((st = wd_v_zero(ctx, xs.v, nh)) != WD_OK) return st;
+    double2 red[2];
+    if ((st = wd_red_norm2(ctx, src, n, 1)) != WD_OK) return st;
+    if ((st = wd_red_fetch(ctx, 2, red)) != WD_OK) return st;
+    const double norm_b = red[1].x > 0 ? std::sqrt(red[1].x) : 1.0;
+
+    // reliable update: x_e += x_s; s = bhat - Mhat x_e; r = Mhat^dag s; r_s, p <- r (p only on restart)
+    double rr = 0, ss = 0;
+    auto reliable = [&](bool reset_p) -> wd_status {
+        wd_status e = mx.accum(xs.v, x_e);
+        if (e != WD_OK) return e;
+        if ((e = wd_apply_Mhat_v(ctx, lat, x_e, t_h.v, tmp_oh.v, m, 0)) != WD_OK) return e;
+        if ((e = wd_v_xpayz(ctx, bhat.v, make_double2(-1.0, 0.0), t_h.v, s_e.v, nh)) != WD_OK) return e;
+        if ((e = wd_apply_Mhat_v(ctx, lat, s_e.v, r_h.v, tmp_oh.v, m, 1)) != WD_OK) return e;
+        if ((e = wd_v_norm2(ctx, r_h.v, nh, 0)) != WD_OK) return e;
+        if ((e = wd_v_norm2(ctx, s_e.v, nh, 1)) != WD_OK) return e;
+        double2 v[2];
+        if ((e = wd_red_fetch(ctx, 2, v)) != WD_OK) return e;
+        rr = v[0].x;
+        ss = v[1].x;
+        // r_s <- r (and p <- r on a restart); otherwise p is kept
+        return mx.from_h(r_h.v, rs.v, reset_p ? p.v : t.v);
+    };
+
+    if ((st = reliable(true)) != WD_OK) return st;
+    double true_res = std::sqrt(ss) / norm_b;
+    double ratio = ss > 0 ? std::sqrt(rr / ss) : 1.0;
+    double target = prm->tol * norm_b * ratio * 0.5;
+    double rr_max = rr;
+    int iters = 0;
+    bool converged = true_res <= prm->tol;
+    while (!converged && iters < prm->max_iter) {
+        if ((st = wd_apply_Mhat_v(ctx, lat, p.v, t.v, tmp_ol.v, m, 0)) != WD_OK) return st;
+        if ((st = wd_apply_Mhat_v(ctx, lat, t.v, q.v, tmp_ol.v, m, 1)) != WD_OK) return st;
+        if ((st = mx.norm2(t.v)) != WD_OK) return st;
+        if ((st = wd_red_fetch(ctx, 1, red)) != WD_OK) return st;
+        const double alpha = rr / red[0].x;
+        if ((st = mx.update((float)alpha, p.v, q.v, xs.v, rs.v)) != WD_OK) return st;
+        if ((st = wd_red_fetch(ctx, 1, red)) != WD_OK) return st;
+        double rr_new = red[0].x;
+        ++iters;
+        if (!std::isfinite(rr_new) || !std::isfinite(alpha)) {
+            stats->iterations = iters;
+            return wd_fail(ctx, WD_ERR_NAN, "mixed CG residual is not finite");
+        }
+        if (rr_new < delta * delta * rr_max || std::sqrt(rr_new) <= target) {
+            const double rr_old = rr;
+            if ((st = reliable(false)) != WD_OK) return st;
+            stats->reliable_updates++;
+            true_res = std::sqrt(ss) / norm_b;
+            if (true_res <= prm->tol) {
+                converged = true;
+                break;
+            }
+            if (std::sqrt(rr_new) <= target) {
+                ratio = ss > 0 ? std::sqrt(rr / ss) : ratio;
+                target = std::fmin(target * 0.5, prm->tol * norm_b * ratio * 0.5);
+            }
+            rr_new = rr;  // continue from the recomputed residual
+            rr_max = rr;
+            rr = rr_old;
+        }
+        const double beta = rr_new / rr;
+        rr = rr_new;
+        if ((st = mx.xpay(rs.v, (float)beta, p.v)) != WD_OK) return st;
+    }
+    if (!converged && (st = mx.accum(xs.v, x_e)) != WD_OK) return st;
+    // x_o = (b_o + D_oe x_e / 2) / a, then back to FP64
+    if ((st = wd_hop_v(ctx, lat, x_e, x_o, &b_o, 1, 0, 0.5 / a, 1.0 / a)) != WD_OK) return st;
+    if (H == WD_PREC_DF64 && (st = wd_convert_df_to_f64(ctx, (const float4 *)hx.v.p, x, n)) != WD_OK) return st;
+    stats->iterations = iters;
+    stats->residual = true_res;
+    stats->converged = converged;
+    return WD_OK;
 }

@@ -34,7 +34,8 @@ class WilsonError(RuntimeError):
 
 class SolverParams(C.Structure):
     _fields_ = [("kind", C.c_int), ("mass", C.c_double), ("tol", C.c_double), ("max_iter", C.c_int),
-                ("prec", C.c_int), ("delta", C.c_double), ("use_initial_guess", C.c_int)]
+                ("prec", C.c_int), ("delta", C.c_double), ("use_initial_guess", C.c_int),
+                ("prec_reliable", C.c_int)]
 
 
 class SolverStats(C.Structure):
@@ -64,6 +65,8 @@ def _load() -> C.CDLL:
         "wd_lattice_destroy": (None, [vp]),
         "wd_lattice_volume": (C.c_int64, [vp]),
         "wd_field_create": (C.c_int, [vp, vp, C.POINTER(vp)]),
+        "wd_field_create_prec": (C.c_int, [vp, vp, C.c_int, C.POINTER(vp)]),
+        "wd_field_precision": (C.c_int, [vp]),
         "wd_field_destroy": (None, [vp]),
         "wd_field_upload": (C.c_int, [vp, vp, vp]),
         "wd_field_download": (C.c_int, [vp, vp, vp]),
@@ -240,8 +243,8 @@ class Lattice:
         except Exception:
             pass
 
-    def field(self, host: np.ndarray | None = None) -> "Field":
-        f = Field(self)
+    def field(self, host: np.ndarray | None = None, prec: int = F64) -> "Field":
+        f = Field(self, prec)
         if host is not None:
             f.upload(host)
         return f
@@ -279,10 +282,11 @@ class Lattice:
 class Field:
     """Resident FP64 spinor field over the full lattice."""
 
-    def __init__(self, lat: Lattice):
+    def __init__(self, lat: Lattice, prec: int = F64):
         self.lat = lat
+        self.prec = prec
         h = C.c_void_p()
-        lat.ctx.check(lib.wd_field_create(lat.ctx.handle, lat.handle, C.byref(h)))
+        lat.ctx.check(lib.wd_field_create_prec(lat.ctx.handle, lat.handle, int(prec), C.byref(h)))
         self.handle = h
 
     def upload(self, host: np.ndarray) -> None:
@@ -324,9 +328,11 @@ class Field:
 
 
 def solver_params(kind: int = CG_EO, mass: float = 0.1, tol: float = 1e-10, max_iter: int = 1000,
-                  prec: int = F64, delta: float = 0.1, use_initial_guess: bool = False) -> SolverParams:
+                  prec: int = F64, delta: float = 0.1, use_initial_guess: bool = False,
+                  prec_reliable: int = F64) -> SolverParams:
     p = SolverParams()
     lib.wd_solver_params_default(C.byref(p))
     p.kind, p.mass, p.tol, p.max_iter, p.prec, p.delta = kind, mass, tol, max_iter, prec, delta
     p.use_initial_guess = int(use_initial_guess)
+    p.prec_reliable = prec_reliable
     return p
