@@ -156,6 +156,31 @@ def cpu_baseline_port(gauge, src, dims, seconds: float = 12.0) -> dict:
                       f"{dt * 1e3:.1f} ms each, C restatement with OpenMP over sites"}
 
 
+def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10) -> dict:
+    """One solve per arithmetic on the resident lattice: solves/s, iterations,
+    FP64 true residual, and the relative difference to the FP64 solution."""
+    b = lat.field(src)
+    out = {}
+    ref = None
+    plans = [("f64", wd.F64, wd.F64), ("df64", wd.DF64, wd.F64), ("mixed_f32", wd.F32, wd.F64),
+             ("mixed_f16", wd.F16, wd.F64), ("mixed_f16_df64", wd.F16, wd.DF64)]
+    for name, prec, rel in plans:
+        x = lat.field()
+        p = wd.solver_params(kind=wd.CG_EO, mass=mass, tol=tol, max_iter=5000, prec=prec, prec_reliable=rel)
+        lat.solve(b, x, p)            # warm-up (derived link copies, allocator)
+        x.zero()
+        st = lat.solve(b, x, p)
+        sol = x.download()
+        if ref is None:
+            ref = sol
+        out[name] = {"solves_per_s": 1.0 / st.seconds, "seconds": st.seconds, "iterations": st.iterations,
+                     "reliable_updates": st.reliable_updates, "true_residual": st.true_residual,
+                     "rel_diff_vs_f64": float(np.linalg.norm(sol - ref) / np.linalg.norm(ref))}
+        x.close()
+    out["speedup_mixed_f16_vs_f64"] = out["f64"]["seconds"] / out["mixed_f16"]["seconds"]
+    return out
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -297,6 +322,10 @@ def run_ours(args) -> None:
             "gpu_launches": launches,
             "clocks": clk,
         }
+        if not args.no_solver:
+            line["solver"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, dims))}, "
+                                          f"mass {MASS}, seed 2",
+                              **solver_bench(wd, ctx, lat, src, MASS)}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_port(gauge, src, dims)
         print(json.dumps(line), flush=True)
@@ -314,6 +343,7 @@ def main() -> None:
                     help="storage/arithmetic of the timed kernel (e2e always uses the FP64 drop-in path)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-solver", action="store_true", help="skip the CG solves/s measurements")
     ap.add_argument("--dims", type=int, nargs=4, default=list(DIMS),
                     help="lattice extents (default 32 32 32 64, the benchmark configuration)")
     args = ap.parse_args()

@@ -188,6 +188,19 @@ wd_status wd_dot_noalloc(const double *a, const double *b, int64_t n, double *ou
  * counts two flops).  Used as the compute roof of the hopping kernels. */
 wd_status wd_diag_fma_peak(wd_context *ctx, double *fp64_tflops, double *fp32_tflops);
 
+/* DslashEEOONew / DslashEE / DslashOO (src/dslash_new.cpp:1301, src/dslash.cpp:11-35) on
+ * host arrays: dest = (4+mass) src on parity `parity` (0 even, 1 odd; the other
+ * half of dest is zeroed) or on both halves (parity = -1). */
+wd_status wd_host_dslash_eeoo(wd_context *ctx, const int dims[4], const double *src, double *dest, double mass,
+                              int parity);
+/* norm_2 / vector_p on host arrays of n complex doubles (any layout):
+ * copied to the device and reduced there in FP64, deterministic order. */
+wd_status wd_host_norm2(wd_context *ctx, int64_t n, const double *a, double *out);
+wd_status wd_host_dot(wd_context *ctx, int64_t n, const double *a, const double *b, double out[2]);
+/* check (src/check.cpp:28-110) on host arrays in the reference layout; out as wd_check. */
+wd_status wd_host_check(wd_context *ctx, const int dims[4], const double *const gauge[4], const double *b,
+                        const double *x, double mass, double out[12]);
+
 /* ---- seeded synthetic inputs (host, deterministic) ---------------------- */
 /* Gauge links U = exp(i eps H) re-unitarised to SU(3), H Gaussian traceless
  * hermitian; written in the reference layout (4 arrays of V*9 complex). */

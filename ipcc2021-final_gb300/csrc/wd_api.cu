@@ -428,16 +428,41 @@ extern "C" wd_status wd_dot(wd_context *ctx, const wd_field *a, const wd_field *
 // ------------------------------------------------------- host-buffer path
 // The reference's functions take host arrays on every call.  The device copy
 // of the links is kept between calls and refreshed when the caller passes a
-// different gauge array (pointer identity) or different extents; callers that
-// rewrite a gauge array in place call wd_lattice_update on their own lattice.
+// different gauge array (pointer identity), different extents, or when a
+// fingerprint of 1024 sampled doubles per direction changes (catches links
+// reloaded in place; a change that touches none of the sampled entries is
+// missed, so callers that edit single links call wd_lattice_update on a
+// lattice of their own).
+static uint64_t gauge_fingerprint(const int dims[4], const double *const gauge[4])
+{
+    const int64_t n = (int64_t)dims[0] * dims[1] * dims[2] * dims[3] * 18;
+    const int64_t step = n > 1024 ? n / 1024 : 1;
+    uint64_t h = 1469598103934665603ull;
+    for (int mu = 0; mu < 4; ++mu)
+        for (int64_t i = 0; i < n; i += step) {
+            uint64_t v;
+            memcpy(&v, gauge[mu] + i, sizeof(v));
+            h = (h ^ v) * 1099511628211ull;
+        }
+    return h;
+}
+
 static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *const gauge[4])
 {
     if (!ctx || !dims || !gauge) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    for (int i = 0; i < 4; ++i)
+        if (!gauge[i] || dims[i] <= 0) return wd_fail(ctx, WD_ERR_BAD_ARG, "bad gauge pointer or extent");
     bool same = ctx->host_lat != nullptr;
     if (same)
         for (int i = 0; i < 4; ++i)
             same = same && ctx->host_lat->g.L[i] == dims[i] && ctx->host_gauge_ptr[i] == gauge[i];
-    if (same) return WD_OK;
+    const uint64_t print = gauge_fingerprint(dims, gauge);
+    if (same && print == ctx->host_gauge_print) return WD_OK;
+    if (same) {  // same arrays, new contents: refresh the links only
+        wd_status st = upload_gauge(ctx, ctx->host_lat, gauge);
+        if (st == WD_OK) ctx->host_gauge_print = print;
+        return st;
+    }
     host_cache_drop(ctx);
     wd_status st = wd_lattice_create(ctx, dims, gauge, &ctx->host_lat);
     if (st != WD_OK) return st;
@@ -449,6 +474,7 @@ static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *
         }
     }
     for (int i = 0; i < 4; ++i) ctx->host_gauge_ptr[i] = gauge[i];
+    ctx->host_gauge_print = print;
     return WD_OK;
 }
 
@@ -489,4 +515,75 @@ extern "C" wd_status wd_host_cg(wd_context *ctx, const int dims[4], const double
     if (solve != WD_OK && solve != WD_ERR_NOT_CONVERGED) return solve;
     st = wd_field_download(ctx, ctx->host_f[1], dest);
     return st != WD_OK ? st : solve;
+}
+
+// reductions of host arrays: staged through the context's staging buffer
+static wd_status host_reduce(wd_context *ctx, int64_t n, const double *a, const double *b, double2 *out)
+{
+    if (!ctx || !a || n < 0) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    const size_t bytes = (size_t)n * sizeof(double2);
+    wd_status st = ensure_staging(ctx, b ? 2 * bytes : bytes);
+    if (st != WD_OK) return st;
+    double2 *da = (double2 *)ctx->staging, *db = da + n;
+    WD_CUDA(ctx, cudaMemcpyAsync(da, a, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    if (b) {
+        WD_CUDA(ctx, cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        st = wd_red_dot(ctx, da, db, n, 0);
+    } else {
+        st = wd_red_norm2(ctx, da, n, 0);
+    }
+    if (st != WD_OK) return st;
+    return wd_red_fetch(ctx, 1, out);
+}
+
+extern "C" wd_status wd_host_norm2(wd_context *ctx, int64_t n, const double *a, double *out)
+{
+    if (!out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    double2 r;
+    wd_status st = host_reduce(ctx, n, a, nullptr, &r);
+    *out = r.x;
+    return st;
+}
+
+extern "C" wd_status wd_host_dot(wd_context *ctx, int64_t n, const double *a, const double *b, double out[2])
+{
+    if (!out || !b) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    double2 r;
+    wd_status st = host_reduce(ctx, n, a, b, &r);
+    out[0] = r.x;
+    out[1] = r.y;
+    return st;
+}
+
+extern "C" wd_status wd_host_check(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                                   const double *b, const double *x, double mass, double out[12])
+{
+    wd_status st = host_prepare(ctx, dims, gauge);
+    if (st != WD_OK) return st;
+    if (!b || !x || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if ((st = wd_field_upload(ctx, ctx->host_f[0], b)) != WD_OK) return st;
+    if ((st = wd_field_upload(ctx, ctx->host_f[1], x)) != WD_OK) return st;
+    return wd_check(ctx, ctx->host_lat, ctx->host_f[0], ctx->host_f[1], mass, out);
+}
+
+extern "C" wd_status wd_host_dslash_eeoo(wd_context *ctx, const int dims[4], const double *src, double *dest,
+                                         double mass, int parity)
+{
+    if (!ctx || !dims || !src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if (parity < -1 || parity > 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "parity must be -1, 0 or 1");
+    WdGeom g;
+    int64_t V;
+    wd_status st = make_geom(ctx, dims, &g, &V);
+    if (st != WD_OK) return st;
+    // reference layout: parity p occupies complex entries [p*Vh*12, (p+1)*Vh*12)
+    const int64_t n = V * 12, nh = n / 2;
+    if ((st = ensure_staging(ctx, n * sizeof(double2))) != WD_OK) return st;
+    double2 *d = (double2 *)ctx->staging;
+    WD_CUDA(ctx, cudaMemcpyAsync(d, src, n * sizeof(double2), cudaMemcpyHostToDevice, ctx->stream));
+    const int64_t lo = parity == 1 ? nh : 0, hi = parity == 0 ? nh : n;
+    if ((st = wd_blas_scale(ctx, 4.0 + mass, d + lo, d + lo, hi - lo)) != WD_OK) return st;
+    if (parity >= 0) WD_CUDA(ctx, cudaMemsetAsync(d + (parity == 0 ? nh : 0), 0, nh * sizeof(double2), ctx->stream));
+    WD_CUDA(ctx, cudaMemcpyAsync(dest, d, n * sizeof(double2), cudaMemcpyDeviceToHost, ctx->stream));
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return WD_OK;
 }

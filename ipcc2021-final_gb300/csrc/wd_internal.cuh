@@ -37,6 +37,7 @@ struct wd_context {
     // cached host-buffer path state (wd_host_*): one lattice + fields
     wd_lattice *host_lat = nullptr;
     const double *host_gauge_ptr[4] = {nullptr, nullptr, nullptr, nullptr};
+    uint64_t host_gauge_print = 0;  // sampled fingerprint of the cached links
     wd_field *host_f[3] = {nullptr, nullptr, nullptr};
 };
 

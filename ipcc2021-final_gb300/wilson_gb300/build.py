@@ -22,6 +22,7 @@ INCLUDE = REPO / "include"
 BUILD = REPO / "_build"
 LIB = PKG / "libwilson_gb300.so"
 COMPAT_LIB = PKG / "liblattice_gb300.so"
+MAIN_BIN = PKG / "wilson_main"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp",
@@ -82,12 +83,21 @@ def build_compat(verbose: bool = False) -> Path:
     srcs = sorted((COMPAT / "src").glob("*.cpp"))
     if not srcs:
         return lib
-    deps = srcs + sorted((COMPAT / "include").glob("*.h")) + [lib]
+    deps = srcs + sorted((COMPAT / "include").glob("*.h")) + sorted((COMPAT / "src").glob("*.h")) + [lib]
     if _stale(COMPAT_LIB, deps):
         cmd = ["g++"] + CXX_FLAGS + ["-I" + str(COMPAT / "include"), "-shared", "-o", str(COMPAT_LIB)] + \
               [str(s) for s in srcs] + ["-L" + str(PKG), "-lwilson_gb300", "-Wl,-rpath,$ORIGIN"]
         _run(cmd)
+    main_src = COMPAT / "wilson_main.cpp"
+    if _stale(MAIN_BIN, [main_src, COMPAT_LIB]):
+        _run(compat_program_cmd(main_src, MAIN_BIN))
     return COMPAT_LIB
+
+
+def compat_program_cmd(src: Path, out: Path) -> list[str]:
+    """g++ command that builds a program against the reference-API layer."""
+    return ["g++", "-O2", "-std=c++17", "-I" + str(COMPAT / "include"), "-o", str(out), str(src),
+            "-L" + str(PKG), "-llattice_gb300", "-lwilson_gb300", "-Wl,-rpath," + str(PKG)]
 
 
 if __name__ == "__main__":

@@ -61,6 +61,7 @@ class Oracle:
         L.wo_dot.argtypes, L.wo_dot.restype = [vp, vp, C.c_long, C.POINTER(C.c_double)], None
         L.wo_srand.argtypes, L.wo_srand.restype = [C.c_uint], None
         L.wo_rand_guess.argtypes, L.wo_rand_guess.restype = [vp, C.c_long], None
+        L.wo_rand_fill.argtypes, L.wo_rand_fill.restype = [vp, C.c_long], None
         L.wo_cg_ref.argtypes = [vp, vp, d4, ip, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.wo_cg_ref.restype = C.c_int
         L.wo_check.argtypes, L.wo_check.restype = [vp, vp, d4, ip, C.c_double, C.POINTER(C.c_double)], None
@@ -97,6 +98,18 @@ class Oracle:
         self.lib.wo_srand(seed)
         self.lib.wo_rand_guess(_p(x), n)
         return x
+
+    def main_inputs(self, dims, seed: int) -> tuple[np.ndarray, np.ndarray]:
+        """The source and CG initial guess the reference's main() draws from
+        one rand() stream after srand(seed) (src/main.cpp:77-94, src/invert.cpp:42-44)."""
+        V = int(np.prod(dims))
+        raw = np.empty(V * 24, np.float64)
+        self.lib.wo_srand(seed)
+        self.lib.wo_rand_fill(C.c_void_p(raw.ctypes.data), raw.size)
+        src = np.ascontiguousarray(raw[0::2] + 1j * raw[1::2])
+        x0 = np.empty(V * 12, np.complex128)
+        self.lib.wo_rand_guess(_p(x0), x0.size)
+        return src, x0
 
     def cg_ref(self, src, gauge, dims, mass, max_iter, accuracy, x0) -> tuple[np.ndarray, int, float]:
         x = np.array(x0, dtype=np.complex128, copy=True)

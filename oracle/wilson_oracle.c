@@ -249,6 +249,14 @@ void wo_dot(const double *a, const double *b, long n, double *out)
     out[1] = im;
 }
 
+/* n values rand()/RAND_MAX from the current rand() stream: the source of
+ * src/main.cpp:82-85 (re, im interleaved) after srand(rank + seed). */
+void wo_rand_fill(double *out, long n)
+{
+    for (long i = 0; i < n; ++i)
+        out[i] = (double)rand() / RAND_MAX;
+}
+
 /* Fill the CG initial guess as src/invert.cpp:42-44 does: real part rand()/RAND_MAX. */
 void wo_srand(unsigned seed) { srand(seed); }
 void wo_rand_guess(double *x, long n)

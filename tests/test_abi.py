@@ -72,3 +72,38 @@ def test_context_without_matching_gpu_reports_no_device(wd):
 def test_null_arguments_are_rejected(wd):
     assert wd.lib.wd_context_create(0, None) == wd.BAD_ARG
     assert wd.lib.wd_solve(None, None, None, None, None, None) == wd.BAD_ARG
+
+
+def test_reference_api_symbols_exported():
+    """liblattice_gb300.so exports the reference's C++ entry points with its signatures."""
+    import subprocess
+    lib = REPO / "ipcc2021-final_gb300" / "wilson_gb300" / "liblattice_gb300.so"
+    out = subprocess.run(["nm", "-DC", "--defined-only", str(lib)], capture_output=True, text=True).stdout
+    for sig in ["DslashNew(lattice_fermion&, lattice_fermion&, lattice_gauge&, double, bool)",
+                "Dslash(lattice_fermion&, lattice_fermion&, lattice_gauge&, double, bool)",
+                "DslashoffdNew(lattice_fermion&, lattice_fermion&, lattice_gauge&, bool, int)",
+                "Dslashoffd(lattice_fermion&, lattice_fermion&, lattice_gauge&, bool, int)",
+                "DslashEEOONew(lattice_fermion&, lattice_fermion&, double)",
+                "DslashEE(lattice_fermion&, lattice_fermion&, double)",
+                "DslashOO(lattice_fermion&, lattice_fermion&, double)",
+                "DslashEONew(lattice_fermion&, lattice_fermion&, lattice_gauge&, bool)",
+                "DslashOENew(lattice_fermion&, lattice_fermion&, lattice_gauge&, bool)",
+                "CGinvert(lattice_fermion&, lattice_fermion&, lattice_gauge&, double, int, double)",
+                "CGinvert(std::complex<double>*, std::complex<double>*, std::complex<double>**, double, int, "
+                "double, int*, int*)",
+                "check(lattice_fermion&, lattice_fermion&, lattice_gauge&, double)",
+                "load_gauge(std::complex<double>**, std::__cxx11::basic_string<char, std::char_traits<char>, "
+                "std::allocator<char> >&, int*, int*)",
+                "lattice_fermion::lattice_fermion(int*, int*)",
+                "lattice_gauge::peeksite(int const*, int, int, int)"]:
+        assert sig in out, sig
+
+
+def test_driver_rejects_bad_arguments_before_touching_a_gpu():
+    import subprocess
+    exe = REPO / "ipcc2021-final_gb300" / "wilson_gb300" / "wilson_main"
+    r = subprocess.run([str(exe), "0.1", "UNIT"], capture_output=True, text=True)
+    assert r.returncode == 1 and "wilson_main Mass gaugefile" in r.stderr
+    r = subprocess.run([str(exe), "0.1", "UNIT", "8", "8", "8", "8", "8", "8", "4", "8"], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "subgrid == lattice" in r.stderr

@@ -1,0 +1,95 @@
+"""The reference-API C++ layer (liblattice_gb300.so) driven from C++ as the
+reference's own callers use it: every operator on the golden inputs, the
+CG with the reference's srand/rand initial guess, and the command-line driver
+against the oracle."""
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import rel_l2
+
+pytestmark = pytest.mark.gpu
+REPO = Path(__file__).resolve().parent.parent
+TOL = 1e-13
+
+
+def _build_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("wd_build", REPO / "ipcc2021-final_gb300/wilson_gb300/build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.build_compat()
+    return mod
+
+
+@pytest.fixture(scope="module")
+def golden_prog(tmp_path_factory):
+    b = _build_module()
+    exe = tmp_path_factory.mktemp("cpp") / "compat_golden"
+    subprocess.run(b.compat_program_cmd(REPO / "tests/cpp/compat_golden.cpp", exe), check=True)
+    return exe
+
+
+def test_reference_api_on_golden_vectors(wd, oracle, golden4, golden_prog, tmp_path):
+    g = golden4
+    V = int(np.prod(g["dims"]))
+    inp, out = tmp_path / "in.bin", tmp_path / "out.bin"
+    with open(inp, "wb") as f:
+        np.array(g["dims"], np.int32).tofile(f)
+        np.array([g["mass"]], np.float64).tofile(f)
+        np.array([int(g["cg_seed"])], np.int32).tofile(f)
+        for u in g["gauge"]:
+            u.tofile(f)
+        g["src"].tofile(f)
+    r = subprocess.run([str(golden_prog), str(inp), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    data = np.fromfile(out, np.uint8)
+    n = V * 12 * 16
+    vecs = [data[i * n:(i + 1) * n].view(np.complex128) for i in range(12)]
+    tail = data[12 * n:]
+    norm2 = tail[:8].view(np.float64)[0]
+    dot = tail[8:24].view(np.complex128)[0]
+    x = tail[24:24 + n].view(np.complex128)
+    names = ["offd_new_dag0_cb0", "offd_new_dag0_cb1", "offd_new_dag1_cb0", "offd_new_dag1_cb1",
+             "full_new_dag0", "full_new_dag1", "full_old_dag0", "eeoo_new", "offd_new_dag0_cb0",
+             "offd_new_dag1_cb1"]
+    for v, k in zip(vecs, names):
+        assert rel_l2(v, g[k]) < TOL, k
+    half = V * 6
+    ee = g["eeoo_new"].copy()
+    ee[half:] = 0
+    oo = g["eeoo_new"].copy()
+    oo[:half] = 0
+    assert rel_l2(vecs[10], ee) == 0.0 and rel_l2(vecs[11], oo) == 0.0
+    assert abs(norm2 - np.vdot(g["src"], g["src"]).real) < 1e-14
+    ref_dot = np.vdot(g["src"], g["full_new_dag0"])
+    assert abs(dot - ref_dot) < 1e-13 * abs(ref_dot)
+    # CGinvert with srand(cg_seed): the reference's own run gave cg_iters / cg_x
+    m = re.search(r"CG: (\d+) iterations, convergence residual \|r\| = ([0-9.eE+-]+)", r.stdout)
+    assert m and int(m.group(1)) == int(g["cg_iters"]), r.stdout
+    assert rel_l2(x, g["cg_x"]) < 1e-10
+
+
+def test_command_line_driver_matches_oracle(wd, oracle):
+    b = _build_module()
+    dims, seed, mass = (4, 4, 4, 8), 3, 0.1
+    r = subprocess.run([str(b.MAIN_BIN), str(mass), "RANDOM", *map(str, dims), *map(str, dims), str(seed)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout
+    src, x0 = oracle.main_inputs(dims, seed)
+    gauge = wd.gen_gauge(dims, 1, 0.5)            # "RANDOM" with the default seed 1
+    x, iters, rsd = oracle.cg_ref(src, gauge, dims, mass, 500, 1e-9, x0)
+    m = re.search(r"CG: (\d+) iterations, convergence residual \|r\| = ([0-9.eE+-]+)", out)
+    assert m, out
+    assert abs(int(m.group(1)) - iters) <= 1
+    chk = oracle.check(src, x, gauge, dims, mass)
+    got_b = float(re.search(r"\|b\| = ([0-9.eE+-]+)", out).group(1))
+    got_res = float(re.search(r"\|M x -b\| = ([0-9.eE+-]+)", out).group(1))
+    assert abs(got_b - chk[0]) < 1e-5 * chk[0]
+    assert got_res < 1e-6 * chk[0] and chk[10] < 1e-6 * chk[0]
+    for line in ("Source and Gauge, time:", "CG invert, time:", "Total time:", "|M^dagger M x - Mdb| ="):
+        assert line in out
