@@ -6,48 +6,122 @@
 // (wd_df.cuh): ~8.5k FP32 operations per site instead of ~890 FP64 ones.
 // Results agree with FP64 to ~1e-14 relative L2 (storage rounding 2^-49,
 // arithmetic ~2^-48 per operation).
+//
+// Colour-split mapping: three threads share an output site, one per colour
+// c.  Each loads only spin components (k, c) of the neighbour and row c (or
+// column c, backward) of the link, projects its colour, and receives the
+// other two colours of the half-spinor from its partners by warp shuffles.
+// Loads stay non-redundant, registers fall from ~144 to ~90 per thread and
+// three times as many threads are in flight to hide memory latency.  A warp
+// holds 10 sites (lanes 0-9 colour 0, 10-19 colour 1, 20-29 colour 2).
 #include "wd_hop.cuh"
 #include "wd_df.cuh"
 #include "wd_kernels.h"
 
 namespace {
 
-struct HopDF {
-    using C = dfc;
-    static constexpr int kThreads = 128;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kSitesPerWarp = 10;
+constexpr int kSplitWarps = 4;
+
+struct SplitDF {
     WdGeom g;
     int cb;
-    const float4 *__restrict__ in;     // parity 1-cb block [12][Vh]
-    const float4 *__restrict__ gauge;  // [4][2][9][Vh]
-    const float4 *__restrict__ x;      // parity cb block or null
-    float4 *__restrict__ out;          // parity cb block
+    const float4 *__restrict__ in;
+    const float4 *__restrict__ gauge;
+    const float4 *__restrict__ x;
+    float4 *__restrict__ out;
     dfr alpha, beta;
-
-    __device__ __forceinline__ void load_in(int s, C *v) const
-    {
-#pragma unroll
-        for (int c = 0; c < 12; ++c) v[c] = df_from_f4(in[(size_t)c * g.Vh + s]);
-    }
-    __device__ __forceinline__ void load_link(int mu, int par, int s, C *U) const
-    {
-        const float4 *b = gauge + (size_t)((mu * 2 + par) * 9) * g.Vh + s;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) U[k] = df_from_f4(b[(size_t)k * g.Vh]);
-    }
-    __device__ __forceinline__ void epilogue(int s, const C *acc) const
-    {
-#pragma unroll
-        for (int c = 0; c < 12; ++c) {
-            dfc r{df_mul(alpha, acc[c].re), df_mul(alpha, acc[c].im)};
-            if (x) {
-                const dfc v = df_from_f4(x[(size_t)c * g.Vh + s]);
-                r.re = df_madd(r.re, beta, v.re);
-                r.im = df_madd(r.im, beta, v.im);
-            }
-            out[(size_t)c * g.Vh + s] = df_to_f4(r);
-        }
-    }
 };
+
+__device__ __forceinline__ dfc shfl_dfc(const dfc &v, int src)
+{
+    return dfc{{__shfl_sync(kFull, v.re.h, src), __shfl_sync(kFull, v.re.l, src)},
+               {__shfl_sync(kFull, v.im.h, src), __shfl_sync(kFull, v.im.l, src)}};
+}
+
+__device__ __forceinline__ dfc ld(const float4 *p, size_t i, bool on)
+{
+    return on ? df_from_f4(p[i]) : c_zero(dfc());
+}
+
+template <int MU, bool FWD, bool DAG>
+__device__ __forceinline__ void split_dir(const SplitDF &p, int s, const WdSite &cs, int col, int c1, int c2,
+                                          int src1, int src2, bool on, dfc *acc)
+{
+    constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
+    const size_t Vh = p.g.Vh;
+    const int nb = wd_neighbour(p.g, s, cs, MU, FWD);
+    dfc h0, h1;
+    {
+        const dfc s0 = ld(p.in, (0 + col) * Vh + nb, on), s1 = ld(p.in, (3 + col) * Vh + nb, on);
+        const dfc s2 = ld(p.in, (6 + col) * Vh + nb, on), s3 = ld(p.in, (9 + col) * Vh + nb, on);
+        wd_proj1<MU, SG>(s0, s1, s2, s3, h0, h1);
+    }
+    // W[col][b] for b = col, c1, c2: forward row col of U_mu(x); backward
+    // conj of column col of U_mu(x - mu)
+    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? s : nb);
+    dfc wa, wb, wc;
+    if constexpr (FWD) {
+        wa = ld(gb, (size_t)(col * 3 + col) * Vh, on);
+        wb = ld(gb, (size_t)(col * 3 + c1) * Vh, on);
+        wc = ld(gb, (size_t)(col * 3 + c2) * Vh, on);
+    } else {
+        wa = ld(gb, (size_t)(col * 3 + col) * Vh, on);
+        wb = ld(gb, (size_t)(c1 * 3 + col) * Vh, on);
+        wc = ld(gb, (size_t)(c2 * 3 + col) * Vh, on);
+    }
+    const dfc h0b = shfl_dfc(h0, src1), h1b = shfl_dfc(h1, src1);
+    const dfc h0c = shfl_dfc(h0, src2), h1c = shfl_dfc(h1, src2);
+    dfc t0, t1;
+    if constexpr (FWD) {
+        t0 = c_madd(c_madd(c_mul(wa, h0), wb, h0b), wc, h0c);
+        t1 = c_madd(c_madd(c_mul(wa, h1), wb, h1b), wc, h1c);
+    } else {
+        t0 = c_maddc(c_maddc(c_mulc(wa, h0), wb, h0b), wc, h0c);
+        t1 = c_maddc(c_maddc(c_mulc(wa, h1), wb, h1b), wc, h1c);
+    }
+    wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
+}
+
+template <bool DAG>
+__global__ void __launch_bounds__(32 * kSplitWarps) k_hop_df_split(const SplitDF p)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int cq = lane / kSitesPerWarp;          // 0..2, 3 for the two idle lanes
+    const int ls = lane - cq * kSitesPerWarp;     // site within the warp
+    const int s_raw = (blockIdx.x * kSplitWarps + warp) * kSitesPerWarp + ls;
+    const bool on = cq < 3 && s_raw < p.g.Vh;
+    const int col = cq < 3 ? cq : 0;
+    const int s = on ? s_raw : 0;                 // idle lanes compute on site 0 and store nothing
+    const int c1 = col == 2 ? 0 : col + 1, c2 = col == 0 ? 2 : col - 1;
+    const int src1 = ls + kSitesPerWarp * c1, src2 = ls + kSitesPerWarp * c2;
+    const WdSite cs = wd_site(p.g, s, p.cb);
+    dfc acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfc());
+    split_dir<0, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    split_dir<0, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    split_dir<1, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    split_dir<1, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    split_dir<2, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    split_dir<2, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    split_dir<3, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    split_dir<3, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
+    if (!on) return;
+    const size_t Vh = p.g.Vh;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t i = (size_t)(k * 3 + col) * Vh + s;
+        dfc r{df_mul(p.alpha, acc[k].re), df_mul(p.alpha, acc[k].im)};
+        if (p.x) {
+            const dfc v = df_from_f4(p.x[i]);
+            r.re = df_madd(r.re, p.beta, v.re);
+            r.im = df_madd(r.im, p.beta, v.im);
+        }
+        p.out[i] = df_to_f4(r);
+    }
+}
 
 __global__ void k_f64_to_df(const double2 *__restrict__ in, float4 *__restrict__ out, int64_t n)
 {
@@ -74,7 +148,7 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
 {
     wd_status st = wd_lattice_gauge_df(ctx, lat);
     if (st != WD_OK) return st;
-    HopDF p;
+    SplitDF p;
     p.g = lat->g;
     p.cb = cb;
     p.in = in_block;
@@ -83,10 +157,10 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
     p.out = out_block;
     p.alpha = df_split(alpha);
     p.beta = df_split(beta);
-    const int threads = HopDF::kThreads;
-    const int blocks = (lat->g.Vh + threads - 1) / threads;
-    if (dag) wd_hop_kernel<true><<<blocks, threads, 0, ctx->stream>>>(p);
-    else wd_hop_kernel<false><<<blocks, threads, 0, ctx->stream>>>(p);
+    const int sites_per_block = kSitesPerWarp * kSplitWarps;
+    const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
+    if (dag) k_hop_df_split<true><<<blocks, 32 * kSplitWarps, 0, ctx->stream>>>(p);
+    else k_hop_df_split<false><<<blocks, 32 * kSplitWarps, 0, ctx->stream>>>(p);
     WD_LAUNCHED(ctx);
     return WD_OK;
 }

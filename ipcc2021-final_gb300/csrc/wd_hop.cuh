@@ -22,51 +22,60 @@ __device__ __forceinline__ C wd_addsg(const C &a, const C &b)
     else return c_sub(a, b);
 }
 
-// Spin projection psi -> (h0, h1) for direction MU, sign SG (see wd_internal.cuh).
+// Spin projection of one colour: (s0, s1, s2, s3) -> (h0, h1) for direction
+// MU and sign SG (the table in wd_internal.cuh).
+template <int MU, int SG, class C>
+__device__ __forceinline__ void wd_proj1(const C &s0, const C &s1, const C &s2, const C &s3, C &h0, C &h1)
+{
+    if constexpr (MU == 0) {
+        h0 = wd_addsg<SG>(s0, c_i(s3));
+        h1 = wd_addsg<SG>(s1, c_i(s2));
+    } else if constexpr (MU == 1) {
+        h0 = wd_addsg<-SG>(s0, s3);
+        h1 = wd_addsg<SG>(s1, s2);
+    } else if constexpr (MU == 2) {
+        h0 = wd_addsg<SG>(s0, c_i(s2));
+        h1 = wd_addsg<-SG>(s1, c_i(s3));
+    } else {
+        h0 = wd_addsg<SG>(s0, s2);
+        h1 = wd_addsg<SG>(s1, s3);
+    }
+}
+
+// Accumulate (t0, t1) = W (h0, h1) of one colour into its four spin components d[0..3].
+template <int MU, int SG, class C>
+__device__ __forceinline__ void wd_recon1(const C &t0, const C &t1, C &d0, C &d1, C &d2, C &d3)
+{
+    d0 = c_add(d0, t0);
+    d1 = c_add(d1, t1);
+    if constexpr (MU == 0) {
+        d2 = wd_addsg<-SG>(d2, c_i(t1));
+        d3 = wd_addsg<-SG>(d3, c_i(t0));
+    } else if constexpr (MU == 1) {
+        d2 = wd_addsg<SG>(d2, t1);
+        d3 = wd_addsg<-SG>(d3, t0);
+    } else if constexpr (MU == 2) {
+        d2 = wd_addsg<-SG>(d2, c_i(t0));
+        d3 = wd_addsg<SG>(d3, c_i(t1));
+    } else {
+        d2 = wd_addsg<SG>(d2, t0);
+        d3 = wd_addsg<SG>(d3, t1);
+    }
+}
+
+// Whole-site forms: sp/acc hold 12 components, index spin*3 + colour.
 template <int MU, int SG, class C>
 __device__ __forceinline__ void wd_proj(const C *sp, C *h0, C *h1)
 {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const C s0 = sp[k], s1 = sp[3 + k], s2 = sp[6 + k], s3 = sp[9 + k];
-        if constexpr (MU == 0) {
-            h0[k] = wd_addsg<SG>(s0, c_i(s3));
-            h1[k] = wd_addsg<SG>(s1, c_i(s2));
-        } else if constexpr (MU == 1) {
-            h0[k] = wd_addsg<-SG>(s0, s3);
-            h1[k] = wd_addsg<SG>(s1, s2);
-        } else if constexpr (MU == 2) {
-            h0[k] = wd_addsg<SG>(s0, c_i(s2));
-            h1[k] = wd_addsg<-SG>(s1, c_i(s3));
-        } else {
-            h0[k] = wd_addsg<SG>(s0, s2);
-            h1[k] = wd_addsg<SG>(s1, s3);
-        }
-    }
+    for (int k = 0; k < 3; ++k) wd_proj1<MU, SG>(sp[k], sp[3 + k], sp[6 + k], sp[9 + k], h0[k], h1[k]);
 }
 
-// Accumulate (t0, t1) = W (h0, h1) into the four spin components.
 template <int MU, int SG, class C>
 __device__ __forceinline__ void wd_recon(const C *t0, const C *t1, C *acc)
 {
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        acc[a] = c_add(acc[a], t0[a]);
-        acc[3 + a] = c_add(acc[3 + a], t1[a]);
-        if constexpr (MU == 0) {
-            acc[6 + a] = wd_addsg<-SG>(acc[6 + a], c_i(t1[a]));
-            acc[9 + a] = wd_addsg<-SG>(acc[9 + a], c_i(t0[a]));
-        } else if constexpr (MU == 1) {
-            acc[6 + a] = wd_addsg<SG>(acc[6 + a], t1[a]);
-            acc[9 + a] = wd_addsg<-SG>(acc[9 + a], t0[a]);
-        } else if constexpr (MU == 2) {
-            acc[6 + a] = wd_addsg<-SG>(acc[6 + a], c_i(t0[a]));
-            acc[9 + a] = wd_addsg<SG>(acc[9 + a], c_i(t1[a]));
-        } else {
-            acc[6 + a] = wd_addsg<SG>(acc[6 + a], t0[a]);
-            acc[9 + a] = wd_addsg<SG>(acc[9 + a], t1[a]);
-        }
-    }
+    for (int a = 0; a < 3; ++a) wd_recon1<MU, SG>(t0[a], t1[a], acc[a], acc[3 + a], acc[6 + a], acc[9 + a]);
 }
 
 // One of the eight neighbour terms.
