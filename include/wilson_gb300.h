@@ -150,6 +150,21 @@ void wd_solver_params_default(wd_solver_params *p);
 wd_status wd_solve(wd_context *ctx, const wd_lattice *lat, const wd_field *src, wd_field *dest,
                    const wd_solver_params *params, wd_solver_stats *stats);
 
+/* Many systems solved together (multi-RHS on one lattice, and lattices of
+ * uneven volume, in any mix): system i solves M(lats[i], masses[i]) x = b on
+ * srcs[i] -> dests[i] (FP64 fields).  Systems on the same lattice handle
+ * share link loads.  Mixed-precision even-odd CG: params->prec = WD_PREC_F32
+ * or WD_PREC_F16 inner operator, params->prec_reliable for the reliable
+ * updates, params->tol the relative true residual of every system.  One
+ * batched launch per operator application covers all systems; iterations
+ * run as a captured CUDA graph with per-system convergence masking.
+ * stats (nsys entries, may be NULL) receive each system's counts and FP64
+ * true residual.  Systems need no relation to the reference; this entry
+ * point has no counterpart there (it replaces a loop of CGinvert calls). */
+wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice *const *lats, const wd_field *const *srcs,
+                         wd_field *const *dests, const double *masses, const wd_solver_params *params,
+                         wd_solver_stats *stats);
+
 /* check (src/check.cpp:28-110): out[0]=|b| out[1]=|x| out[2..3]=(Mb,Mb) out[4..5]=(b,M^dag M b)
  * out[6..7]=(Mx,Mx) out[8..9]=(x,M^dag M x) out[10]=|Mx-b| out[11]=|M^dag M x - M^dag b| */
 wd_status wd_check(wd_context *ctx, const wd_lattice *lat, const wd_field *b, const wd_field *x,

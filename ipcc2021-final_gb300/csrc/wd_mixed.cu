@@ -199,6 +199,16 @@ inline WdVec par_half(WdVec v, int par, int Vh) { return wd_offset(v, (int64_t)p
 
 }  // namespace
 
+wd_status wd_mx_accum(wd_context *ctx, int Vh, wd_precision H, WdVec xs, WdVec xh)
+{
+    return Mixed{ctx, Vh, WD_PREC_F32, H}.accum(xs, xh);
+}
+
+wd_status wd_mx_from_h(wd_context *ctx, int Vh, wd_precision L, wd_precision H, WdVec h, WdVec rs, WdVec p)
+{
+    return Mixed{ctx, Vh, L, H}.from_h(h, rs, p);
+}
+
 wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const double2 *src, double2 *x,
                                const wd_solver_params *prm, wd_solver_stats *stats)
 {

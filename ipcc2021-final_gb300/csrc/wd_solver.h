@@ -24,3 +24,8 @@ wd_status wd_true_residual(wd_context *ctx, const wd_lattice *lat, const double2
 // mixed-precision (FP32 / FP16 inner) even-odd CG with reliable updates
 wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const double2 *src, double2 *x,
                                const wd_solver_params *prm, wd_solver_stats *stats);
+// reliable-update pieces shared by the mixed solvers (wd_mixed.cu):
+// xh (FP64 or double-float) += xs (FP32), xs = 0
+wd_status wd_mx_accum(wd_context *ctx, int Vh, wd_precision H, WdVec xs, WdVec xh);
+// rs (FP32) <- h and p (storage L) <- h
+wd_status wd_mx_from_h(wd_context *ctx, int Vh, wd_precision L, wd_precision H, WdVec h, WdVec rs, WdVec p);

@@ -82,6 +82,8 @@ def _load() -> C.CDLL:
         "wd_solver_params_default": (None, [C.POINTER(SolverParams)]),
         "wd_solve": (C.c_int, [vp, vp, vp, vp, C.POINTER(SolverParams), C.POINTER(SolverStats)]),
         "wd_check": (C.c_int, [vp, vp, vp, vp, C.c_double, dp]),
+        "wd_solve_batch": (C.c_int, [vp, C.c_int, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), dp,
+                                     C.POINTER(SolverParams), C.POINTER(SolverStats)]),
         "wd_host_dslash_offd": (C.c_int, [vp, ip, d4, vp, vp, C.c_int, C.c_int]),
         "wd_host_dslash_full": (C.c_int, [vp, ip, d4, vp, vp, C.c_double, C.c_int]),
         "wd_host_cg": (C.c_int, [vp, ip, d4, vp, vp, C.POINTER(SolverParams), C.POINTER(SolverStats)]),
@@ -194,6 +196,19 @@ class Context:
 
     def lattice(self, dims, gauge) -> "Lattice":
         return Lattice(self, dims, gauge)
+
+    def solve_batch(self, systems, params: SolverParams, allow_unconverged: bool = False) -> list[SolverStats]:
+        """systems: sequence of (lattice, src Field, dest Field, mass).  Returns per-system stats."""
+        n = len(systems)
+        lats = (C.c_void_p * n)(*[s[0].handle.value for s in systems])
+        srcs = (C.c_void_p * n)(*[s[1].handle.value for s in systems])
+        dsts = (C.c_void_p * n)(*[s[2].handle.value for s in systems])
+        masses = (C.c_double * n)(*[float(s[3]) for s in systems])
+        stats = (SolverStats * n)()
+        st = lib.wd_solve_batch(self.handle, n, lats, srcs, dsts, masses, C.byref(params), stats)
+        if not (allow_unconverged and st == NOT_CONVERGED):
+            self.check(st)
+        return list(stats)
 
     # host-buffer entry points (reference layout in and out)
     def host_dslash_offd(self, dims, gauge, src: np.ndarray, dag: bool, cb: int) -> np.ndarray:
