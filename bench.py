@@ -181,6 +181,85 @@ def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10) -> dict:
     return out
 
 
+def batch_bench(wd, ctx) -> dict:
+    """Batched solves against the same systems solved one at a time.
+    (a) one 24^3x48 lattice (seed 3, mass 0.05): 12 point sources (unit delta at
+        site 0 for each spin/colour) + 12 Gaussian sources;
+    (b) 16 lattices, L in {8,12,16,24} (four each), T = 2L, independent seeds,
+        masses uniform in [0.05, 0.2], one Gaussian source each.
+    All to FP64 true residual 1e-10 with the mixed FP32 solver."""
+    import time as _t
+
+    def run(systems, params):
+        for _, _, x, _ in systems:
+            x.zero()
+        ctx.sync()
+        stats = ctx.solve_batch(systems, params)
+        assert all(st.converged and st.true_residual <= 1e-10 for st in stats)
+        return stats[0].seconds, stats   # the solve; the FP64 check of each result follows it
+
+    def solo(systems, prec, rel):
+        total, worst = 0.0, 0.0
+        for lat, b, x, m in systems:
+            x.zero()
+            st = lat.solve(b, x, wd.solver_params(kind=wd.CG_EO, mass=m, tol=1e-10, max_iter=5000, prec=prec,
+                                                  prec_reliable=rel))
+            worst = max(worst, st.true_residual)
+            total += st.seconds
+        return total, worst
+
+    out = {}
+    dims = (24, 24, 24, 48)
+    V = int(np.prod(dims))
+    lat = ctx.lattice(dims, wd.gen_gauge(dims, 3, EPS))
+    srcs = []
+    for s_ in range(4):
+        for c in range(3):
+            b = np.zeros(V * 12, np.complex128)
+            b[s_ * 3 + c] = 1.0
+            srcs.append(b)
+    srcs += [wd.gen_source(dims, 1000 + k) for k in range(12)]
+    systems = [(lat, lat.field(b), lat.field(), 0.05) for b in srcs]
+    res = {}
+    for name, rel in (("f32_inner_f64_reliable", wd.F64), ("f32_inner_df64_reliable", wd.DF64)):
+        p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=rel)
+        run(systems, p)  # warm-up
+        dt, stats = run(systems, p)
+        res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt,
+                     "max_iterations": max(st.iterations for st in stats),
+                     "max_true_residual": max(st.true_residual for st in stats)}
+    for name, prec, rel in (("solo_mixed_f32", wd.F32, wd.F64), ("solo_f64", wd.F64, wd.F64)):
+        dt, worst = solo(systems, prec, rel)
+        res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt, "max_true_residual": worst}
+    res["speedup_batched_vs_solo_f64"] = res["solo_f64"]["seconds"] / res["f32_inner_f64_reliable"]["seconds"]
+    out["multi_rhs_24c48_24_sources"] = res
+    for _, b, x, _ in systems:
+        b.close()
+        x.close()
+    lat.close()
+
+    rng = np.random.default_rng(4)
+    systems, lats = [], []
+    for i, L in enumerate([8, 12, 16, 24] * 4):
+        d = (L, L, L, 2 * L)
+        la = ctx.lattice(d, wd.gen_gauge(d, 200 + i, EPS))
+        lats.append(la)
+        systems.append((la, la.field(wd.gen_source(d, 300 + i)), la.field(), float(rng.uniform(0.05, 0.2))))
+    res = {}
+    p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=wd.F64)
+    run(systems, p)
+    dt, stats = run(systems, p)
+    res["batched"] = {"seconds": dt, "solves_per_s": len(systems) / dt,
+                      "iterations": [st.iterations for st in stats],
+                      "max_true_residual": max(st.true_residual for st in stats)}
+    for name, prec, rel in (("solo_mixed_f32", wd.F32, wd.F64), ("solo_f64", wd.F64, wd.F64)):
+        dt, worst = solo(systems, prec, rel)
+        res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt, "max_true_residual": worst}
+    res["speedup_batched_vs_solo_f64"] = res["solo_f64"]["seconds"] / res["batched"]["seconds"]
+    out["16_lattices_L8_to_24"] = res
+    return out
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -326,6 +405,8 @@ def run_ours(args) -> None:
             line["solver"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, dims))}, "
                                           f"mass {MASS}, seed 2",
                               **solver_bench(wd, ctx, lat, src, MASS)}
+        if not args.no_batch:
+            line["batch"] = batch_bench(wd, ctx)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_port(gauge, src, dims)
         print(json.dumps(line), flush=True)
@@ -344,6 +425,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true", help="skip the CG solves/s measurements")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurements")
     ap.add_argument("--dims", type=int, nargs=4, default=list(DIMS),
                     help="lattice extents (default 32 32 32 64, the benchmark configuration)")
     args = ap.parse_args()

@@ -83,11 +83,56 @@ static void host_cache_drop(wd_context *ctx)
     for (auto &p : ctx->host_gauge_ptr) p = nullptr;
 }
 
+wd_status wd_dev_alloc(wd_context *ctx, void **p, size_t bytes)
+{
+    bytes = (bytes + 255) & ~(size_t)255;
+    // best fit among cached blocks no more than twice the request
+    auto it = ctx->pool_free.lower_bound(bytes);
+    if (it != ctx->pool_free.end() && it->first <= 2 * bytes) {
+        *p = it->second;
+        ctx->pool_used[it->second] = it->first;
+        ctx->pool_free.erase(it);
+        return WD_OK;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        wd_pool_release(ctx);
+        e = cudaMalloc(p, bytes);
+    }
+    if (e != cudaSuccess) return wd_cuda_check(ctx, e, "cudaMalloc(work buffer)");
+    ctx->pool_used[*p] = bytes;
+    ctx->pool_bytes += bytes;
+    return WD_OK;
+}
+
+void wd_dev_free(wd_context *ctx, void *p)
+{
+    if (!p) return;
+    auto it = ctx->pool_used.find(p);
+    if (it == ctx->pool_used.end()) return;
+    ctx->pool_free.emplace(it->second, p);
+    ctx->pool_used.erase(it);
+}
+
+void wd_pool_release(wd_context *ctx)
+{
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &kv : ctx->pool_free) {
+        cudaFree(kv.second);
+        ctx->pool_bytes -= kv.first;
+    }
+    ctx->pool_free.clear();
+}
+
 extern "C" void wd_context_destroy(wd_context *ctx)
 {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     host_cache_drop(ctx);
+    wd_pool_release(ctx);
+    for (auto &kv : ctx->pool_used) cudaFree(kv.first);
+    ctx->pool_used.clear();
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->red_partial);
     cudaFree(ctx->staging);

@@ -274,12 +274,16 @@ template <class T>
 struct DevArray {
     T *p = nullptr;
     size_t n = 0;
-    ~DevArray() { cudaFree(p); }
-    wd_status alloc(wd_context *ctx, size_t count)
+    wd_context *ctx = nullptr;
+    ~DevArray()
+    {
+        if (ctx) wd_dev_free(ctx, p);
+    }
+    wd_status alloc(wd_context *c, size_t count)
     {
         n = count;
-        WD_CUDA(ctx, cudaMalloc(&p, count * sizeof(T)));
-        return WD_OK;
+        ctx = c;
+        return wd_dev_alloc(c, (void **)&p, count * sizeof(T));
     }
     wd_status put(wd_context *ctx, const std::vector<T> &h)
     {
@@ -587,7 +591,6 @@ extern "C" wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice 
     }
 
     // ---- finish: fold x_s, reconstruct x_o, write the FP64 solutions
-    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     for (int k = 0; k < nsys; ++k) {
         const int i = sys_of_slot[k];
         const wd_lattice *lat = lats[i];
@@ -609,6 +612,8 @@ extern "C" wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice 
             WD_CUDA(ctx, cudaMemcpyAsync(dests[i]->d, B.hx.v.p, 2 * nh * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
         }
     }
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     bool all = true;
     for (int k = 0; k < nsys; ++k) {
         const int i = sys_of_slot[k];
@@ -619,11 +624,11 @@ extern "C" wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice 
         s.converged = sb[k].converged;
         s.seconds = secs;
         if (stats) {
-            // FP64 true residual of each returned solution
-            double2 *tmp = nullptr;
-            WD_CUDA(ctx, cudaMalloc((void **)&tmp, (size_t)lats[i]->volume * 12 * sizeof(double2)));
-            st = wd_true_residual(ctx, lats[i], srcs[i]->d, dests[i]->d, tmp, masses[i], &s.true_residual);
-            cudaFree(tmp);
+            // FP64 true residual of each returned solution (a check, after the timed solve)
+            WdVecBuf tmp;
+            if ((st = wd_vec_alloc(ctx, tmp, WD_PREC_F64, lats[i]->volume * 12)) != WD_OK) return st;
+            st = wd_true_residual(ctx, lats[i], srcs[i]->d, dests[i]->d, (double2 *)tmp.v.p, masses[i],
+                                  &s.true_residual);
             if (st != WD_OK) return st;
             stats[i] = s;
         }

@@ -12,7 +12,9 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <map>
 #include <string>
+#include <unordered_map>
 #include "../../include/wilson_gb300.h"
 
 #define WD_MAX_SITES (int64_t(1) << 30)
@@ -39,7 +41,18 @@ struct wd_context {
     const double *host_gauge_ptr[4] = {nullptr, nullptr, nullptr, nullptr};
     uint64_t host_gauge_print = 0;  // sampled fingerprint of the cached links
     wd_field *host_f[3] = {nullptr, nullptr, nullptr};
+    // caching allocator for solver work buffers: blocks freed by one call are
+    // reused by the next in stream order (one stream per context)
+    std::multimap<size_t, void *> pool_free;
+    std::unordered_map<void *, size_t> pool_used;
+    size_t pool_bytes = 0;
 };
+
+// Work-buffer allocation through the context's cache (stream-ordered reuse;
+// on allocation failure the cached blocks are released and the call retried).
+wd_status wd_dev_alloc(wd_context *ctx, void **p, size_t bytes);
+void wd_dev_free(wd_context *ctx, void *p);
+void wd_pool_release(wd_context *ctx);
 
 struct wd_lattice {
     wd_context *ctx = nullptr;

@@ -23,7 +23,9 @@ wd_status wd_vec_alloc(wd_context *ctx, WdVecBuf &b, wd_precision prec, int64_t 
     b.release();
     size_t bytes = (size_t)n_complex * wd_entry_bytes(prec);
     if (prec == WD_PREC_F16) bytes += (size_t)(n_complex / 12) * sizeof(float);
-    WD_CUDA(ctx, cudaMalloc(&b.v.p, bytes));
+    wd_status st = wd_dev_alloc(ctx, &b.v.p, bytes);
+    if (st != WD_OK) return st;
+    b.ctx = ctx;
     b.v.prec = prec;
     b.v.scale = prec == WD_PREC_F16 ? (float *)((char *)b.v.p + (size_t)n_complex * wd_entry_bytes(prec)) : nullptr;
     return WD_OK;
@@ -31,8 +33,9 @@ wd_status wd_vec_alloc(wd_context *ctx, WdVecBuf &b, wd_precision prec, int64_t 
 
 void WdVecBuf::release()
 {
-    cudaFree(v.p);
+    if (ctx) wd_dev_free(ctx, v.p);
     v = WdVec{};
+    ctx = nullptr;
 }
 
 // half of a full-lattice vector (parity 0 or 1)
@@ -305,10 +308,10 @@ extern "C" wd_status wd_solve(wd_context *ctx, const wd_lattice *lat, const wd_f
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     // the FP64 true residual |b - M x|/|b| of whatever the solver returned
-    double2 *tmp = nullptr;
-    WD_CUDA(ctx, cudaMalloc((void **)&tmp, (size_t)lat->volume * 12 * sizeof(double2)));
-    st = wd_true_residual(ctx, lat, src->d, dest->d, tmp, params->mass, &stats->true_residual);
-    cudaFree(tmp);
+    // (a check of the result, after the timed solve)
+    WdVecBuf tmp;
+    if ((st = wd_vec_alloc(ctx, tmp, WD_PREC_F64, lat->volume * 12)) != WD_OK) return st;
+    st = wd_true_residual(ctx, lat, src->d, dest->d, (double2 *)tmp.v.p, params->mass, &stats->true_residual);
     if (st != WD_OK) return st;
     return stats->converged ? WD_OK : WD_ERR_NOT_CONVERGED;
 }

@@ -5,6 +5,7 @@
 // A device vector owned by a solver (freed on scope exit).
 struct WdVecBuf {
     WdVec v;
+    wd_context *ctx = nullptr;  // owner of the cached block
     WdVecBuf() = default;
     WdVecBuf(const WdVecBuf &) = delete;
     WdVecBuf &operator=(const WdVecBuf &) = delete;
