@@ -165,6 +165,35 @@ wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice *const *lat
                          wd_field *const *dests, const double *masses, const wd_solver_params *params,
                          wd_solver_stats *stats);
 
+/* ---- serving: continuous batching of solve requests (no counterpart in the reference) ---- */
+typedef struct wd_server wd_server;
+typedef struct wd_server_config {
+    wd_precision prec;          /* WD_PREC_F32 / WD_PREC_F16: batched mixed precision;
+                                   WD_PREC_F64: the plain FP64 solver, one system at a time */
+    wd_precision prec_reliable; /* reliable updates of the mixed solver: WD_PREC_F64 or WD_PREC_DF64 */
+    double hbm_budget_bytes;    /* admission limit: resident links + admitted requests */
+    int max_systems;            /* right-hand sides iterating together */
+    int max_iter;
+    double delta;               /* reliable-update threshold (0 -> 0.1) */
+} wd_server_config;
+void wd_server_config_default(wd_server_config *c);
+wd_status wd_server_create(wd_context *ctx, const wd_server_config *cfg, wd_server **server);
+void wd_server_destroy(wd_server *server);
+/* make a gauge field resident (reference layout); its derived link copies count against the budget */
+wd_status wd_server_add_lattice(wd_server *server, const int dims[4], const double *const gauge[4], int *lattice_id);
+/* queue a request of nsrc right-hand sides: host sources (reference layout), or, when sources is
+ * NULL, unit-norm Gaussian sources generated on the device from seeds[k]; WD_ERR_OOM if it could
+ * never fit the budget. */
+wd_status wd_server_submit(wd_server *server, int lattice_id, int nsrc, const double *const *sources,
+                           const uint64_t *seeds, double mass, double tol, int64_t *request_id);
+/* admit queued requests that fit, advance every admitted system by one quantum, retire finished ones */
+wd_status wd_server_step(wd_server *server, int *completed);
+/* done: 1 when finished; then solutions (nsrc host arrays, may be NULL), stats (nsrc) and the
+ * submit-to-finish latency are returned and the request's device memory is released */
+wd_status wd_server_poll(wd_server *server, int64_t request_id, int *done, double *const *solutions,
+                         wd_solver_stats *stats, double *latency_s);
+wd_status wd_server_status(const wd_server *server, int *queued, int *active_systems, double *bytes_in_use);
+
 /* check (src/check.cpp:28-110): out[0]=|b| out[1]=|x| out[2..3]=(Mb,Mb) out[4..5]=(b,M^dag M b)
  * out[6..7]=(Mx,Mx) out[8..9]=(x,M^dag M x) out[10]=|Mx-b| out[11]=|M^dag M x - M^dag b| */
 wd_status wd_check(wd_context *ctx, const wd_lattice *lat, const wd_field *b, const wd_field *x,

@@ -18,8 +18,12 @@
 // and their kernels return at once.  Between replays the host reads the
 // per-system residuals and runs reliable updates (double-float or FP64) for
 // the systems that need one -- the same recurrence as wd_mixed.cu.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <deque>
+#include <map>
+#include <memory>
 #include <vector>
 #include "wd_df.cuh"
 #include "wd_hop.cuh"
@@ -258,16 +262,26 @@ __global__ void k_batch_scalars(const BVec *v, BState st, int nsys, int mode)
 
 }  // namespace
 
-// ====================================================== host-side solver
+// ====================================================== the batch engine
+//
+// BatchEngine keeps a changing set of systems iterating together.  Systems
+// are added with add() (set-up and the first reliable update run at once)
+// and step() advances every active system by one captured graph of
+// per_graph iterations, then reads the per-system residuals, runs reliable
+// updates where due and retires converged systems (writes the FP64 solution
+// and frees their buffers).  A retired system is first masked in the device
+// tables; the tables and the graph are rebuilt (compacted) when systems join
+// or when masked systems make up half of the tables.
 
 namespace {
 
 struct SysBufs {
-    WdVecBuf p, t, q, tmp_o, rs, xs;                       // low precision / FP32
-    WdVecBuf hs, hx, bhat, s_e, r_h, t_h, tmp_oh;          // high precision
-    double norm_b = 1, rr_max = 0, target = 0, ratio = 1, true_res = 1;
-    int updates = 0, iters = 0;
-    bool converged = false;
+    WdVecBuf p, t, q, tmp_o, rs, xs;               // kernel storage / FP32
+    WdVecBuf hs, hx, bhat, s_e, r_h, t_h, tmp_oh;  // high precision
+    void release()
+    {
+        for (WdVecBuf *b : {&p, &t, &q, &tmp_o, &rs, &xs, &hs, &hx, &bhat, &s_e, &r_h, &t_h, &tmp_oh}) b->release();
+    }
 };
 
 template <class T>
@@ -275,25 +289,445 @@ struct DevArray {
     T *p = nullptr;
     size_t n = 0;
     wd_context *ctx = nullptr;
-    ~DevArray()
+    DevArray() = default;
+    DevArray(const DevArray &) = delete;
+    DevArray &operator=(const DevArray &) = delete;
+    ~DevArray() { release(); }
+    void release()
     {
         if (ctx) wd_dev_free(ctx, p);
+        p = nullptr;
+        n = 0;
+        ctx = nullptr;
     }
-    wd_status alloc(wd_context *c, size_t count)
+    wd_status put(wd_context *c, const std::vector<T> &h)
     {
-        n = count;
-        ctx = c;
-        return wd_dev_alloc(c, (void **)&p, count * sizeof(T));
-    }
-    wd_status put(wd_context *ctx, const std::vector<T> &h)
-    {
-        WD_CUDA(ctx, cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+        if (h.size() > n) {
+            release();
+            ctx = c;
+            n = h.size();
+            wd_status st = wd_dev_alloc(c, (void **)&p, n * sizeof(T));
+            if (st != WD_OK) return st;
+        }
+        if (!h.empty())
+            WD_CUDA(c, cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
         return WD_OK;
     }
 };
 
+struct EngineSys {
+    int tag;
+    const wd_lattice *lat;
+    double mass, tol;
+    const double2 *src;  // FP64 source (device, caller-owned)
+    double2 *dest;       // FP64 solution (device, caller-owned)
+    SysBufs B;
+    double norm_b = 1, rr = 0, rr_max = 0, target = 0, ratio = 1, true_res = 1;
+    int updates = 0, iters = 0;
+    bool active = true;
+};
+
+// device bytes of one system's work buffers
+size_t system_bytes(const wd_lattice *lat, wd_precision L, wd_precision H)
+{
+    const size_t nh = (size_t)12 * lat->g.Vh;
+    size_t lbytes = nh * wd_entry_bytes(L) + (L == WD_PREC_F16 ? (size_t)lat->g.Vh * 4 : 0);
+    return 4 * lbytes + 2 * nh * 8 + 5 * nh * wd_entry_bytes(H) + 2 * 2 * nh * wd_entry_bytes(H);
+}
+
+class BatchEngine {
+  public:
+    BatchEngine(wd_context *ctx, wd_precision L, wd_precision H, double delta, int per_graph, int max_iter)
+        : ctx_(ctx), L_(L), H_(H), delta_(delta), per_graph_(per_graph), max_iter_(max_iter)
+    {
+    }
+    ~BatchEngine() { drop_graph(); }
+
+    size_t active() const
+    {
+        size_t n = 0;
+        for (auto &s : sys_) n += s->active;
+        return n;
+    }
+    bool idle() const { return active() == 0; }
+    std::map<int, wd_solver_stats> results;  // tag -> stats of retired systems
+    double solve_seconds = 0;                // time spent in step() and add()
+
+    wd_status add(int tag, const wd_lattice *lat, const double2 *src, double2 *dest, double mass, double tol);
+    // finished (optional) receives the tags retired since the previous call
+    wd_status step(std::vector<int> *finished);
+    void take_retired(std::vector<int> *out)
+    {
+        out->insert(out->end(), retired_.begin(), retired_.end());
+        retired_.clear();
+    }
+
+  private:
+    wd_context *ctx_;
+    wd_precision L_, H_;
+    double delta_;
+    int per_graph_, max_iter_;
+    std::vector<std::unique_ptr<EngineSys>> sys_;
+    std::vector<int> retired_;
+    bool rebuild_ = true, scalars_dirty_ = false;
+    // device tables
+    DevArray<BGroup> d_groups_;
+    DevArray<BSys> d_sys_[4];
+    DevArray<float> d_alpha_[4], d_beta_[4];
+    DevArray<BVec> d_vec_;
+    DevArray<double> d_rr_, d_tt_, d_partial_;
+    DevArray<float> d_a_, d_b_;
+    DevArray<int> d_active_, d_chunk_sys_;
+    int grid_x_ = 0, grid_y_ = 1, nchunks_ = 0, ngroups_ = 0;
+    cudaGraphExec_t exec_ = nullptr;
+    uint64_t kernels_per_graph_ = 0;
+
+    void drop_graph()
+    {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+    }
+    wd_status reliable(EngineSys &s, bool reset_p, double *rr, double *ss);
+    wd_status finish(EngineSys &s);
+    wd_status rebuild();
+    wd_status iteration(const BState &bst);
+    wd_status upload_scalars();
+};
+
+static inline void slices(EngineSys &s, WdVec &b_e, WdVec &b_o, WdVec &x_e, WdVec &x_o)
+{
+    const int Vh = s.lat->g.Vh;
+    b_e = s.B.hs.v;
+    b_o = wd_offset(s.B.hs.v, (int64_t)12 * Vh, Vh);
+    x_e = s.B.hx.v;
+    x_o = wd_offset(s.B.hx.v, (int64_t)12 * Vh, Vh);
+}
+
+// reliable update: x_e += x_s; s = bhat - Mhat x_e; r = Mhat^dag s; r_s <- r (p <- r on a restart)
+wd_status BatchEngine::reliable(EngineSys &s, bool reset_p, double *rr, double *ss)
+{
+    const int Vh = s.lat->g.Vh;
+    const int64_t nh = (int64_t)12 * Vh;
+    SysBufs &B = s.B;
+    WdVec b_e, b_o, x_e, x_o;
+    slices(s, b_e, b_o, x_e, x_o);
+    wd_status e;
+    if ((e = wd_mx_accum(ctx_, Vh, H_, B.xs.v, x_e)) != WD_OK) return e;
+    if ((e = wd_apply_Mhat_v(ctx_, s.lat, x_e, B.t_h.v, B.tmp_oh.v, s.mass, 0)) != WD_OK) return e;
+    if ((e = wd_v_xpayz(ctx_, B.bhat.v, make_double2(-1.0, 0.0), B.t_h.v, B.s_e.v, nh)) != WD_OK) return e;
+    if ((e = wd_apply_Mhat_v(ctx_, s.lat, B.s_e.v, B.r_h.v, B.tmp_oh.v, s.mass, 1)) != WD_OK) return e;
+    if ((e = wd_v_norm2(ctx_, B.r_h.v, nh, 0)) != WD_OK) return e;
+    if ((e = wd_v_norm2(ctx_, B.s_e.v, nh, 1)) != WD_OK) return e;
+    double2 v[2];
+    if ((e = wd_red_fetch(ctx_, 2, v)) != WD_OK) return e;
+    *rr = v[0].x;
+    *ss = v[1].x;
+    // r_s <- r; p <- r on a restart (otherwise t, rewritten next iteration, takes the copy)
+    return wd_mx_from_h(ctx_, Vh, L_, H_, B.r_h.v, B.rs.v, reset_p ? B.p.v : B.t.v);
+}
+
+wd_status BatchEngine::add(int tag, const wd_lattice *lat, const double2 *src, double2 *dest, double mass,
+                           double tol)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    auto sp = std::make_unique<EngineSys>();
+    EngineSys &s = *sp;
+    s.tag = tag, s.lat = lat, s.mass = mass, s.tol = tol, s.src = src, s.dest = dest;
+    const int Vh = lat->g.Vh;
+    const int64_t nh = (int64_t)12 * Vh;
+    const double a = 4.0 + mass;
+    SysBufs &B = s.B;
+    wd_status st;
+    for (WdVecBuf *b : {&B.p, &B.t, &B.q, &B.tmp_o})
+        if ((st = wd_vec_alloc(ctx_, *b, L_, nh)) != WD_OK) return st;
+    for (WdVecBuf *b : {&B.rs, &B.xs})
+        if ((st = wd_vec_alloc(ctx_, *b, WD_PREC_F32, nh)) != WD_OK) return st;
+    for (WdVecBuf *b : {&B.bhat, &B.s_e, &B.r_h, &B.t_h, &B.tmp_oh})
+        if ((st = wd_vec_alloc(ctx_, *b, H_, nh)) != WD_OK) return st;
+    for (WdVecBuf *b : {&B.hs, &B.hx})
+        if ((st = wd_vec_alloc(ctx_, *b, H_, 2 * nh)) != WD_OK) return st;
+    if ((st = wd_lattice_gauge_lp(ctx_, lat, L_)) != WD_OK) return st;
+    if (H_ == WD_PREC_DF64) {
+        if ((st = wd_convert_f64_to_df(ctx_, src, (float4 *)B.hs.v.p, 2 * nh)) != WD_OK) return st;
+    } else {
+        WD_CUDA(ctx_, cudaMemcpyAsync(B.hs.v.p, src, 2 * nh * sizeof(double2), cudaMemcpyDeviceToDevice, ctx_->stream));
+    }
+    WdVec b_e, b_o, x_e, x_o;
+    slices(s, b_e, b_o, x_e, x_o);
+    if ((st = wd_hop_v(ctx_, lat, b_o, B.bhat.v, &b_e, 0, 0, 0.5 / a, 1.0)) != WD_OK) return st;
+    if ((st = wd_v_zero(ctx_, B.hx.v, 2 * nh)) != WD_OK) return st;
+    if ((st = wd_v_zero(ctx_, B.xs.v, nh)) != WD_OK) return st;
+    if ((st = wd_red_norm2(ctx_, src, 2 * nh, 0)) != WD_OK) return st;
+    double2 v;
+    if ((st = wd_red_fetch(ctx_, 1, &v)) != WD_OK) return st;
+    s.norm_b = v.x > 0 ? std::sqrt(v.x) : 1.0;
+    double rr, ss;
+    if ((st = reliable(s, true, &rr, &ss)) != WD_OK) return st;
+    s.true_res = std::sqrt(ss) / s.norm_b;
+    s.ratio = ss > 0 ? std::sqrt(rr / ss) : 1.0;
+    s.target = tol * s.norm_b * s.ratio * 0.5;
+    s.rr = s.rr_max = rr;
+    sys_.push_back(std::move(sp));
+    rebuild_ = true;
+    solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (s.true_res <= tol) return finish(s);  // already solved (e.g. zero source)
+    return WD_OK;
+}
+
+// fold x_s, reconstruct x_o, write the FP64 solution, record stats, free buffers
+wd_status BatchEngine::finish(EngineSys &s)
+{
+    const int Vh = s.lat->g.Vh;
+    const int64_t nh = (int64_t)12 * Vh;
+    const double a = 4.0 + s.mass;
+    WdVec b_e, b_o, x_e, x_o;
+    slices(s, b_e, b_o, x_e, x_o);
+    wd_status st;
+    const bool converged = s.true_res <= s.tol;
+    if ((st = wd_mx_accum(ctx_, Vh, H_, s.B.xs.v, x_e)) != WD_OK) return st;
+    if ((st = wd_hop_v(ctx_, s.lat, x_e, x_o, &b_o, 1, 0, 0.5 / a, 1.0 / a)) != WD_OK) return st;
+    if (H_ == WD_PREC_DF64) {
+        if ((st = wd_convert_df_to_f64(ctx_, (const float4 *)s.B.hx.v.p, s.dest, 2 * nh)) != WD_OK) return st;
+    } else {
+        WD_CUDA(ctx_, cudaMemcpyAsync(s.dest, s.B.hx.v.p, 2 * nh * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                      ctx_->stream));
+    }
+    wd_solver_stats r{};
+    r.iterations = s.iters;
+    r.reliable_updates = s.updates;
+    r.residual = s.true_res;
+    r.converged = converged;
+    results[s.tag] = r;
+    retired_.push_back(s.tag);
+    s.active = false;
+    s.B.release();  // buffers back to the pool
+    scalars_dirty_ = true;
+    return WD_OK;
+}
+
+wd_status BatchEngine::rebuild()
+{
+    drop_graph();
+    // drop retired systems, group by lattice (stable)
+    std::vector<std::unique_ptr<EngineSys>> keep;
+    for (auto &s : sys_)
+        if (s->active) keep.push_back(std::move(s));
+    std::stable_sort(keep.begin(), keep.end(),
+                     [](const std::unique_ptr<EngineSys> &x, const std::unique_ptr<EngineSys> &y) {
+                         return x->lat < y->lat;
+                     });
+    sys_ = std::move(keep);
+    const int nsys = (int)sys_.size();
+    rebuild_ = false;
+    scalars_dirty_ = false;
+    if (nsys == 0) return WD_OK;
+    const bool f16 = L_ == WD_PREC_F16;
+    std::vector<BGroup> groups;
+    int blocks = 0;
+    for (int k = 0; k < nsys; ++k) {
+        if (k == 0 || sys_[k]->lat != sys_[k - 1]->lat) {
+            BGroup G{};
+            G.g = sys_[k]->lat->g;
+            G.gauge = f16 ? sys_[k]->lat->gauge_h12 : sys_[k]->lat->gauge_f32;
+            G.first_sys = k;
+            G.nsys = 0;
+            G.block_start = blocks;
+            blocks += (G.g.Vh + kSites - 1) / kSites;
+            groups.push_back(G);
+        }
+        groups.back().nsys++;
+    }
+    grid_x_ = blocks;
+    grid_y_ = 1;
+    for (const BGroup &G : groups) grid_y_ = std::max(grid_y_, (G.nsys + kSysPerBlock - 1) / kSysPerBlock);
+    ngroups_ = (int)groups.size();
+    std::vector<BVec> bvec(nsys);
+    std::vector<int> chunk_sys;
+    std::vector<double> rr(nsys);
+    std::vector<int> act(nsys, 1);
+    for (int k = 0; k < nsys; ++k) {
+        SysBufs &B = sys_[k]->B;
+        BVec &v = bvec[k];
+        v.p = B.p.v.p, v.t = B.t.v.p, v.q = B.q.v.p;
+        v.p_scale = B.p.v.scale, v.t_scale = B.t.v.scale, v.q_scale = B.q.v.scale;
+        v.rs = (float4 *)B.rs.v.p, v.xs = (float4 *)B.xs.v.p;
+        v.Vh = sys_[k]->lat->g.Vh;
+        v.chunk0 = (int)chunk_sys.size();
+        for (int c = 0; c < (v.Vh + kChunk - 1) / kChunk; ++c) chunk_sys.push_back(k);
+        rr[k] = sys_[k]->rr;
+    }
+    nchunks_ = (int)chunk_sys.size();
+    wd_status st;
+    if ((st = d_groups_.put(ctx_, groups)) != WD_OK) return st;
+    for (int h = 0; h < 4; ++h) {
+        std::vector<BSys> tab(nsys);
+        std::vector<float> al(nsys), be(nsys);
+        for (int k = 0; k < nsys; ++k) {
+            const double a = 4.0 + sys_[k]->mass;
+            const SysBufs &B = sys_[k]->B;
+            // h = 0: p -> tmp_o (cb 1); 1: tmp_o -> t with x = p (cb 0); 2: t -> tmp_o; 3: tmp_o -> q with x = t
+            const WdVec *vin[4] = {&B.p.v, &B.tmp_o.v, &B.t.v, &B.tmp_o.v};
+            const WdVec *vout[4] = {&B.tmp_o.v, &B.t.v, &B.tmp_o.v, &B.q.v};
+            const WdVec *vx[4] = {nullptr, &B.p.v, nullptr, &B.t.v};
+            tab[k] = BSys{vin[h]->p, vout[h]->p, vx[h] ? vx[h]->p : nullptr, vin[h]->scale, vout[h]->scale,
+                          vx[h] ? vx[h]->scale : nullptr, 0};
+            al[k] = (h % 2 == 0) ? 1.0f : (float)(-0.25 / a);
+            be[k] = (h % 2 == 0) ? 0.0f : (float)a;
+        }
+        if ((st = d_sys_[h].put(ctx_, tab)) != WD_OK) return st;
+        if ((st = d_alpha_[h].put(ctx_, al)) != WD_OK) return st;
+        if ((st = d_beta_[h].put(ctx_, be)) != WD_OK) return st;
+    }
+    std::vector<double> zeros_d(nsys, 0.0), zeros_p(2 * (size_t)nchunks_, 0.0);
+    std::vector<float> zeros_f(nsys, 0.f);
+    if ((st = d_vec_.put(ctx_, bvec)) != WD_OK) return st;
+    if ((st = d_rr_.put(ctx_, rr)) != WD_OK) return st;
+    if ((st = d_tt_.put(ctx_, zeros_d)) != WD_OK) return st;
+    if ((st = d_a_.put(ctx_, zeros_f)) != WD_OK) return st;
+    if ((st = d_b_.put(ctx_, zeros_f)) != WD_OK) return st;
+    if ((st = d_active_.put(ctx_, act)) != WD_OK) return st;
+    if ((st = d_partial_.put(ctx_, zeros_p)) != WD_OK) return st;
+    if ((st = d_chunk_sys_.put(ctx_, chunk_sys)) != WD_OK) return st;
+
+    // capture per_graph iterations
+    const BState bst{d_rr_.p, d_tt_.p, d_a_.p, d_b_.p, d_active_.p, d_partial_.p, d_chunk_sys_.p, nchunks_};
+    const uint64_t before = ctx_->launches;
+    cudaGraph_t graph = nullptr;
+    WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
+    WD_CUDA(ctx_, cudaStreamBeginCapture(ctx_->stream, cudaStreamCaptureModeThreadLocal));
+    wd_status cap = WD_OK;
+    for (int k = 0; k < per_graph_ && cap == WD_OK; ++k) cap = iteration(bst);
+    const cudaError_t ce = cudaStreamEndCapture(ctx_->stream, &graph);
+    kernels_per_graph_ = ctx_->launches - before;
+    ctx_->launches = before;  // counted per replay
+    if (cap != WD_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return cap;
+    }
+    if (ce != cudaSuccess) return wd_cuda_check(ctx_, ce, "cudaStreamEndCapture");
+    const cudaError_t ie = cudaGraphInstantiate(&exec_, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        exec_ = nullptr;
+        return wd_cuda_check(ctx_, ie, "cudaGraphInstantiate");
+    }
+    return WD_OK;
+}
+
+wd_status BatchEngine::iteration(const BState &bst)
+{
+    const int nsys = (int)sys_.size();
+    const bool f16 = L_ == WD_PREC_F16;
+    auto hop = [&](int h, int cb, int dag) -> wd_status {
+        const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_active_.p, cb};
+        dim3 grid(grid_x_, grid_y_);
+        const int threads = kSites * kSysPerBlock;
+        if (f16) {
+            if (dag) k_batch_hop<true, true><<<grid, threads, 0, ctx_->stream>>>(t);
+            else k_batch_hop<false, true><<<grid, threads, 0, ctx_->stream>>>(t);
+        } else {
+            if (dag) k_batch_hop<true, false><<<grid, threads, 0, ctx_->stream>>>(t);
+            else k_batch_hop<false, false><<<grid, threads, 0, ctx_->stream>>>(t);
+        }
+        WD_LAUNCHED(ctx_);
+        return WD_OK;
+    };
+    wd_status e;
+    if ((e = hop(0, 1, 0)) != WD_OK || (e = hop(1, 0, 0)) != WD_OK) return e;  // t = Mhat p
+    if ((e = hop(2, 1, 1)) != WD_OK || (e = hop(3, 0, 1)) != WD_OK) return e;  // q = Mhat^dag t
+    if (f16) k_batch_norm_t<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    else k_batch_norm_t<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    WD_LAUNCHED(ctx_);
+    k_batch_scalars<<<(nsys + 127) / 128, 128, 0, ctx_->stream>>>(d_vec_.p, bst, nsys, 0);
+    WD_LAUNCHED(ctx_);
+    if (f16) k_batch_update<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    else k_batch_update<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    WD_LAUNCHED(ctx_);
+    k_batch_scalars<<<(nsys + 127) / 128, 128, 0, ctx_->stream>>>(d_vec_.p, bst, nsys, 1);
+    WD_LAUNCHED(ctx_);
+    if (f16) k_batch_xpay<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    else k_batch_xpay<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    WD_LAUNCHED(ctx_);
+    return WD_OK;
+}
+
+wd_status BatchEngine::upload_scalars()
+{
+    const int nsys = (int)sys_.size();
+    std::vector<double> rr(nsys);
+    std::vector<int> act(nsys);
+    for (int k = 0; k < nsys; ++k) {
+        rr[k] = sys_[k]->rr;
+        act[k] = sys_[k]->active ? 1 : 0;
+    }
+    wd_status st;
+    if ((st = d_rr_.put(ctx_, rr)) != WD_OK) return st;
+    if ((st = d_active_.put(ctx_, act)) != WD_OK) return st;
+    scalars_dirty_ = false;
+    return WD_OK;
+}
+
+wd_status BatchEngine::step(std::vector<int> *finished)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    const size_t before = results.size();
+    wd_status st;
+    // compact when systems joined or half the tables are masked
+    size_t masked = 0;
+    for (auto &s : sys_) masked += !s->active;
+    if (rebuild_ || (masked > 0 && 2 * masked >= sys_.size())) {
+        if ((st = rebuild()) != WD_OK) return st;
+    } else if (scalars_dirty_) {
+        if ((st = upload_scalars()) != WD_OK) return st;
+    }
+    if (sys_.empty() || !exec_) return WD_OK;
+    WD_CUDA(ctx_, cudaGraphLaunch(exec_, ctx_->stream));
+    ctx_->launches += kernels_per_graph_;
+    const int nsys = (int)sys_.size();
+    std::vector<double> rr(nsys);
+    WD_CUDA(ctx_, cudaMemcpyAsync(rr.data(), d_rr_.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, ctx_->stream));
+    WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
+    for (int k = 0; k < nsys; ++k) {
+        EngineSys &s = *sys_[k];
+        if (!s.active) continue;
+        s.iters += per_graph_;
+        const double rr_new = rr[k];
+        if (!std::isfinite(rr_new)) return wd_fail(ctx_, WD_ERR_NAN, "batched CG residual is not finite");
+        s.rr = rr_new;
+        const bool at_target = std::sqrt(rr_new) <= s.target;
+        if (rr_new < delta_ * delta_ * s.rr_max || at_target) {
+            double rrt, ss;
+            if ((st = reliable(s, false, &rrt, &ss)) != WD_OK) return st;
+            s.updates++;
+            s.true_res = std::sqrt(ss) / s.norm_b;
+            if (s.true_res <= s.tol) {
+                if ((st = finish(s)) != WD_OK) return st;
+                continue;
+            }
+            if (at_target) {
+                s.ratio = ss > 0 ? std::sqrt(rrt / ss) : s.ratio;
+                s.target = std::fmin(s.target * 0.5, s.tol * s.norm_b * s.ratio * 0.5);
+            }
+            s.rr = s.rr_max = rrt;  // continue from the recomputed residual
+            scalars_dirty_ = true;
+        }
+        if (s.iters >= max_iter_) {  // give up on this system: return what it has
+            if ((st = finish(s)) != WD_OK) return st;
+        }
+    }
+    WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
+    solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (finished) {
+        finished->clear();
+        take_retired(finished);
+    }
+    (void)before;
+    return WD_OK;
+}
+
 }  // namespace
 
+// ==================================================== one batch, all systems
 extern "C" wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice *const *lats,
                                     const wd_field *const *srcs, wd_field *const *dests, const double *masses,
                                     const wd_solver_params *prm, wd_solver_stats *stats)
@@ -302,326 +736,25 @@ extern "C" wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice 
         return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
     if (prm->prec != WD_PREC_F32 && prm->prec != WD_PREC_F16)
         return wd_fail(ctx, WD_ERR_BAD_ARG, "batched solves run a mixed FP32 or FP16 inner solver");
-    const wd_precision L = prm->prec;
-    const wd_precision H = prm->prec_reliable == WD_PREC_DF64 ? WD_PREC_DF64 : WD_PREC_F64;
-    const bool f16 = L == WD_PREC_F16;
-    const double delta = prm->delta > 0 && prm->delta < 1 ? prm->delta : 0.1;
-    const auto t0 = std::chrono::steady_clock::now();
-    wd_status st;
-
-    // ---- groups: consecutive systems on the same lattice share links
-    std::vector<int> order(nsys);
+    if (prm->max_iter < 1 || !(prm->tol > 0)) return wd_fail(ctx, WD_ERR_BAD_ARG, "bad tolerance or max_iter");
     for (int i = 0; i < nsys; ++i) {
         if (!lats[i] || !srcs[i] || !dests[i]) return wd_fail(ctx, WD_ERR_BAD_ARG, "null system");
-        if (srcs[i]->storage != WD_PREC_F64 || dests[i]->storage != WD_PREC_F64 || srcs[i]->lat->volume != lats[i]->volume ||
-            dests[i]->lat->volume != lats[i]->volume)
+        if (srcs[i]->storage != WD_PREC_F64 || dests[i]->storage != WD_PREC_F64 ||
+            srcs[i]->lat->volume != lats[i]->volume || dests[i]->lat->volume != lats[i]->volume)
             return wd_fail(ctx, WD_ERR_BAD_ARG, "batch fields must be FP64 fields of their system's lattice");
-        order[i] = i;
     }
-    std::vector<BGroup> groups;
-    std::vector<int> sys_of_slot;  // slot -> system index (grouped order)
-    {
-        std::vector<bool> done(nsys, false);
-        int blocks = 0;
-        for (int i = 0; i < nsys; ++i) {
-            if (done[i]) continue;
-            BGroup G{};
-            G.g = lats[i]->g;
-            G.first_sys = (int)sys_of_slot.size();
-            G.block_start = blocks;
-            for (int j = i; j < nsys; ++j)
-                if (!done[j] && lats[j] == lats[i]) {
-                    done[j] = true;
-                    sys_of_slot.push_back(j);
-                }
-            G.nsys = (int)sys_of_slot.size() - G.first_sys;
-            if ((st = wd_lattice_gauge_lp(ctx, lats[i], L)) != WD_OK) return st;
-            G.gauge = f16 ? lats[i]->gauge_h12 : lats[i]->gauge_f32;
-            blocks += (G.g.Vh + kSites - 1) / kSites;
-            groups.push_back(G);
-        }
-    }
-    int grid_y = 1;
-    for (const BGroup &G : groups) grid_y = std::max(grid_y, (G.nsys + kSysPerBlock - 1) / kSysPerBlock);
-    const int grid_x = groups.back().block_start + (groups.back().g.Vh + kSites - 1) / kSites;
-
-    // ---- per-system buffers (slot order)
-    std::vector<SysBufs> sb(nsys);
-    std::vector<BVec> bvec(nsys);
-    std::vector<int> chunk_sys;
-    for (int k = 0; k < nsys; ++k) {
-        const int i = sys_of_slot[k];
-        const wd_lattice *lat = lats[i];
-        const int64_t nh = (int64_t)12 * lat->g.Vh;
-        SysBufs &B = sb[k];
-        for (WdVecBuf *b : {&B.p, &B.t, &B.q, &B.tmp_o})
-            if ((st = wd_vec_alloc(ctx, *b, L, nh)) != WD_OK) return st;
-        for (WdVecBuf *b : {&B.rs, &B.xs})
-            if ((st = wd_vec_alloc(ctx, *b, WD_PREC_F32, nh)) != WD_OK) return st;
-        for (WdVecBuf *b : {&B.bhat, &B.s_e, &B.r_h, &B.t_h, &B.tmp_oh})
-            if ((st = wd_vec_alloc(ctx, *b, H, nh)) != WD_OK) return st;
-        if ((st = wd_vec_alloc(ctx, B.hs, H, 2 * nh)) != WD_OK) return st;
-        if ((st = wd_vec_alloc(ctx, B.hx, H, 2 * nh)) != WD_OK) return st;
-        BVec &v = bvec[k];
-        v.p = B.p.v.p, v.t = B.t.v.p, v.q = B.q.v.p;
-        v.p_scale = B.p.v.scale, v.t_scale = B.t.v.scale, v.q_scale = B.q.v.scale;
-        v.rs = (float4 *)B.rs.v.p, v.xs = (float4 *)B.xs.v.p;
-        v.Vh = lat->g.Vh;
-        v.chunk0 = (int)chunk_sys.size();
-        for (int c = 0; c < (v.Vh + kChunk - 1) / kChunk; ++c) chunk_sys.push_back(k);
-    }
-    const int nchunks = (int)chunk_sys.size();
-
-    // ---- device tables: 4 hop tables (Mhat: p->tmp_o->t, Mhat^dag: t->tmp_o->q)
-    DevArray<BGroup> d_groups;
-    DevArray<BSys> d_sys[4];
-    DevArray<float> d_alpha[4], d_beta[4];
-    DevArray<BVec> d_vec;
-    DevArray<double> d_rr, d_tt, d_partial;
-    DevArray<float> d_a, d_b;
-    DevArray<int> d_active, d_chunk_sys;
-    if ((st = d_groups.alloc(ctx, groups.size())) != WD_OK || (st = d_groups.put(ctx, groups)) != WD_OK) return st;
-    for (int h = 0; h < 4; ++h) {
-        std::vector<BSys> tab(nsys);
-        std::vector<float> al(nsys), be(nsys);
-        for (int k = 0; k < nsys; ++k) {
-            const double a = 4.0 + masses[sys_of_slot[k]];
-            const SysBufs &B = sb[k];
-            const WdVec *in, *out, *x = nullptr;
-            // h = 0: p -> tmp_o (cb 1); 1: tmp_o -> t with x = p (cb 0); 2: t -> tmp_o; 3: tmp_o -> q with x = t
-            const WdVec *vin[4] = {&B.p.v, &B.tmp_o.v, &B.t.v, &B.tmp_o.v};
-            const WdVec *vout[4] = {&B.tmp_o.v, &B.t.v, &B.tmp_o.v, &B.q.v};
-            const WdVec *vx[4] = {nullptr, &B.p.v, nullptr, &B.t.v};
-            in = vin[h], out = vout[h], x = vx[h];
-            tab[k] = BSys{in->p, out->p, x ? x->p : nullptr, in->scale, out->scale, x ? x->scale : nullptr, 0};
-            al[k] = (h % 2 == 0) ? 1.0f : (float)(-0.25 / a);
-            be[k] = (h % 2 == 0) ? 0.0f : (float)a;
-        }
-        if ((st = d_sys[h].alloc(ctx, nsys)) != WD_OK || (st = d_sys[h].put(ctx, tab)) != WD_OK) return st;
-        if ((st = d_alpha[h].alloc(ctx, nsys)) != WD_OK || (st = d_alpha[h].put(ctx, al)) != WD_OK) return st;
-        if ((st = d_beta[h].alloc(ctx, nsys)) != WD_OK || (st = d_beta[h].put(ctx, be)) != WD_OK) return st;
-    }
-    if ((st = d_vec.alloc(ctx, nsys)) != WD_OK || (st = d_vec.put(ctx, bvec)) != WD_OK) return st;
-    if ((st = d_rr.alloc(ctx, nsys)) != WD_OK || (st = d_tt.alloc(ctx, nsys)) != WD_OK) return st;
-    if ((st = d_a.alloc(ctx, nsys)) != WD_OK || (st = d_b.alloc(ctx, nsys)) != WD_OK) return st;
-    if ((st = d_active.alloc(ctx, nsys)) != WD_OK) return st;
-    if ((st = d_partial.alloc(ctx, 2 * (size_t)nchunks)) != WD_OK) return st;
-    if ((st = d_chunk_sys.alloc(ctx, nchunks)) != WD_OK || (st = d_chunk_sys.put(ctx, chunk_sys)) != WD_OK) return st;
-    const BState bst{d_rr.p, d_tt.p, d_a.p, d_b.p, d_active.p, d_partial.p, d_chunk_sys.p, nchunks};
-
-    // ---- per-system set-up and the first (restart) reliable update
-    auto sys_slices = [&](int k, WdVec &b_e, WdVec &b_o, WdVec &x_e, WdVec &x_o) {
-        const int Vh = lats[sys_of_slot[k]]->g.Vh;
-        b_e = sb[k].hs.v;
-        b_o = wd_offset(sb[k].hs.v, (int64_t)12 * Vh, Vh);
-        x_e = sb[k].hx.v;
-        x_o = wd_offset(sb[k].hx.v, (int64_t)12 * Vh, Vh);
-    };
-    std::vector<double> h_rr(nsys), h_rr_last(nsys);
-    std::vector<int> h_active(nsys, 1);
-    // reliable update of system k: x_e += x_s; s = bhat - Mhat x_e; r = Mhat^dag s; r_s, (p) <- r
-    auto reliable = [&](int k, bool reset_p, double *rr, double *ss) -> wd_status {
-        const int i = sys_of_slot[k];
-        const wd_lattice *lat = lats[i];
-        const int Vh = lat->g.Vh;
-        const int64_t nh = (int64_t)12 * Vh;
-        const double m = masses[i];
-        SysBufs &B = sb[k];
-        WdVec b_e, b_o, x_e, x_o;
-        sys_slices(k, b_e, b_o, x_e, x_o);
-        wd_status e;
-        // x_H += x_s; x_s = 0
-        if ((e = wd_mx_accum(ctx, Vh, H, B.xs.v, x_e)) != WD_OK) return e;
-        if ((e = wd_apply_Mhat_v(ctx, lat, x_e, B.t_h.v, B.tmp_oh.v, m, 0)) != WD_OK) return e;
-        if ((e = wd_v_xpayz(ctx, B.bhat.v, make_double2(-1.0, 0.0), B.t_h.v, B.s_e.v, nh)) != WD_OK) return e;
-        if ((e = wd_apply_Mhat_v(ctx, lat, B.s_e.v, B.r_h.v, B.tmp_oh.v, m, 1)) != WD_OK) return e;
-        if ((e = wd_v_norm2(ctx, B.r_h.v, nh, 0)) != WD_OK) return e;
-        if ((e = wd_v_norm2(ctx, B.s_e.v, nh, 1)) != WD_OK) return e;
-        double2 v[2];
-        if ((e = wd_red_fetch(ctx, 2, v)) != WD_OK) return e;
-        *rr = v[0].x;
-        *ss = v[1].x;
-        // r_s <- r (FP32); p <- r on a restart (otherwise t, rewritten next iteration, takes the copy)
-        return wd_mx_from_h(ctx, Vh, L, H, B.r_h.v, B.rs.v, reset_p ? B.p.v : B.t.v);
-    };
-
-    for (int k = 0; k < nsys; ++k) {
-        const int i = sys_of_slot[k];
-        const wd_lattice *lat = lats[i];
-        const int Vh = lat->g.Vh;
-        const int64_t nh = (int64_t)12 * Vh;
-        const double a = 4.0 + masses[i];
-        SysBufs &B = sb[k];
-        if (H == WD_PREC_DF64) {
-            if ((st = wd_convert_f64_to_df(ctx, srcs[i]->d, (float4 *)B.hs.v.p, 2 * nh)) != WD_OK) return st;
-        } else {
-            WD_CUDA(ctx, cudaMemcpyAsync(B.hs.v.p, srcs[i]->d, 2 * nh * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
-        }
-        WdVec b_e, b_o, x_e, x_o;
-        sys_slices(k, b_e, b_o, x_e, x_o);
-        if ((st = wd_hop_v(ctx, lat, b_o, B.bhat.v, &b_e, 0, 0, 0.5 / a, 1.0)) != WD_OK) return st;
-        if ((st = wd_v_zero(ctx, B.hx.v, 2 * nh)) != WD_OK) return st;
-        if ((st = wd_v_zero(ctx, B.xs.v, nh)) != WD_OK) return st;
-        if ((st = wd_red_norm2(ctx, srcs[i]->d, 2 * nh, 0)) != WD_OK) return st;
-        double2 v;
-        if ((st = wd_red_fetch(ctx, 1, &v)) != WD_OK) return st;
-        B.norm_b = v.x > 0 ? std::sqrt(v.x) : 1.0;
-        double rr, ss;
-        if ((st = reliable(k, true, &rr, &ss)) != WD_OK) return st;
-        B.true_res = std::sqrt(ss) / B.norm_b;
-        B.ratio = ss > 0 ? std::sqrt(rr / ss) : 1.0;
-        B.target = prm->tol * B.norm_b * B.ratio * 0.5;
-        B.rr_max = rr;
-        h_rr[k] = rr;
-        B.converged = B.true_res <= prm->tol;
-        h_active[k] = B.converged ? 0 : 1;
-    }
-    if ((st = d_rr.put(ctx, h_rr)) != WD_OK) return st;
-    if ((st = d_active.put(ctx, h_active)) != WD_OK) return st;
-
-    // ---- capture one iteration into a CUDA graph
-    auto hop = [&](int h, int cb, int dag) -> wd_status {
-        const BTable t{d_groups.p, (int)groups.size(), d_sys[h].p, d_alpha[h].p, d_beta[h].p, d_active.p, cb};
-        dim3 grid(grid_x, grid_y);
-        const int threads = kSites * kSysPerBlock;
-        if (f16) {
-            if (dag) k_batch_hop<true, true><<<grid, threads, 0, ctx->stream>>>(t);
-            else k_batch_hop<false, true><<<grid, threads, 0, ctx->stream>>>(t);
-        } else {
-            if (dag) k_batch_hop<true, false><<<grid, threads, 0, ctx->stream>>>(t);
-            else k_batch_hop<false, false><<<grid, threads, 0, ctx->stream>>>(t);
-        }
-        WD_LAUNCHED(ctx);
-        return WD_OK;
-    };
-    auto iteration = [&]() -> wd_status {
-        wd_status e;
-        if ((e = hop(0, 1, 0)) != WD_OK || (e = hop(1, 0, 0)) != WD_OK) return e;  // t = Mhat p
-        if ((e = hop(2, 1, 1)) != WD_OK || (e = hop(3, 0, 1)) != WD_OK) return e;  // q = Mhat^dag t
-        if (f16) k_batch_norm_t<true><<<nchunks, WD_RED_THREADS, 0, ctx->stream>>>(d_vec.p, bst);
-        else k_batch_norm_t<false><<<nchunks, WD_RED_THREADS, 0, ctx->stream>>>(d_vec.p, bst);
-        WD_LAUNCHED(ctx);
-        k_batch_scalars<<<(nsys + 127) / 128, 128, 0, ctx->stream>>>(d_vec.p, bst, nsys, 0);
-        WD_LAUNCHED(ctx);
-        if (f16) k_batch_update<true><<<nchunks, WD_RED_THREADS, 0, ctx->stream>>>(d_vec.p, bst);
-        else k_batch_update<false><<<nchunks, WD_RED_THREADS, 0, ctx->stream>>>(d_vec.p, bst);
-        WD_LAUNCHED(ctx);
-        k_batch_scalars<<<(nsys + 127) / 128, 128, 0, ctx->stream>>>(d_vec.p, bst, nsys, 1);
-        WD_LAUNCHED(ctx);
-        if (f16) k_batch_xpay<true><<<nchunks, WD_RED_THREADS, 0, ctx->stream>>>(d_vec.p, bst);
-        else k_batch_xpay<false><<<nchunks, WD_RED_THREADS, 0, ctx->stream>>>(d_vec.p, bst);
-        WD_LAUNCHED(ctx);
-        return WD_OK;
-    };
-    const int per_graph = 4;  // iterations per graph launch between host checks
-    const uint64_t launches_before_capture = ctx->launches;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    WD_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    wd_status cap = WD_OK;
-    for (int k = 0; k < per_graph && cap == WD_OK; ++k) cap = iteration();
-    const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
-    if (cap != WD_OK) {
-        if (graph) cudaGraphDestroy(graph);
-        return cap;
-    }
-    if (ce != cudaSuccess) return wd_cuda_check(ctx, ce, "cudaStreamEndCapture");
-    const uint64_t kernels_per_graph = ctx->launches - launches_before_capture;
-    ctx->launches = launches_before_capture;  // counted per replay below
-    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess) return wd_cuda_check(ctx, ie, "cudaGraphInstantiate");
-    struct GraphGuard {
-        cudaGraphExec_t e;
-        ~GraphGuard() { cudaGraphExecDestroy(e); }
-    } guard{exec};
-
-    // ---- iterate: graph replays, host checks, reliable updates, masking
-    int iters = 0, graph_launches = 0;
-    std::vector<double> rr_dev(nsys);
-    bool any = false;
-    for (int v : h_active) any = any || v;
-    while (any && iters < prm->max_iter) {
-        h_rr_last.assign(h_rr.begin(), h_rr.end());
-        WD_CUDA(ctx, cudaGraphLaunch(exec, ctx->stream));
-        ctx->launches += kernels_per_graph;
-        ++graph_launches;
-        iters += per_graph;
-        WD_CUDA(ctx, cudaMemcpyAsync(rr_dev.data(), d_rr.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        bool changed = false;
-        any = false;
-        for (int k = 0; k < nsys; ++k) {
-            if (!h_active[k]) continue;
-            SysBufs &B = sb[k];
-            B.iters += per_graph;
-            const double rr_new = rr_dev[k];
-            if (!std::isfinite(rr_new)) return wd_fail(ctx, WD_ERR_NAN, "batched CG residual is not finite");
-            if (rr_new < delta * delta * B.rr_max || std::sqrt(rr_new) <= B.target) {
-                double rr, ss;
-                if ((st = reliable(k, false, &rr, &ss)) != WD_OK) return st;
-                B.updates++;
-                B.true_res = std::sqrt(ss) / B.norm_b;
-                if (B.true_res <= prm->tol) {
-                    B.converged = true;
-                    h_active[k] = 0;
-                    changed = true;
-                    continue;
-                }
-                if (std::sqrt(rr_new) <= B.target) {
-                    B.ratio = ss > 0 ? std::sqrt(rr / ss) : B.ratio;
-                    B.target = std::fmin(B.target * 0.5, prm->tol * B.norm_b * B.ratio * 0.5);
-                }
-                // continue the recurrence from the recomputed residual: beta of
-                // the next iteration uses rr_new over this rr
-                B.rr_max = rr;
-                rr_dev[k] = rr;
-                changed = true;
-            }
-            any = true;
-        }
-        if (changed) {
-            std::vector<double> rr_put(rr_dev.begin(), rr_dev.end());
-            WD_CUDA(ctx, cudaMemcpyAsync(d_rr.p, rr_put.data(), nsys * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-            WD_CUDA(ctx, cudaMemcpyAsync(d_active.p, h_active.data(), nsys * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-            WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        }
-        h_rr.assign(rr_dev.begin(), rr_dev.end());
-    }
-
-    // ---- finish: fold x_s, reconstruct x_o, write the FP64 solutions
-    for (int k = 0; k < nsys; ++k) {
-        const int i = sys_of_slot[k];
-        const wd_lattice *lat = lats[i];
-        const int Vh = lat->g.Vh;
-        const int64_t nh = (int64_t)12 * Vh;
-        const double a = 4.0 + masses[i];
-        SysBufs &B = sb[k];
-        WdVec b_e, b_o, x_e, x_o;
-        sys_slices(k, b_e, b_o, x_e, x_o);
-        if (!B.converged) {
-            double rr, ss;
-            if ((st = reliable(k, false, &rr, &ss)) != WD_OK) return st;
-            B.true_res = std::sqrt(ss) / B.norm_b;
-        }
-        if ((st = wd_hop_v(ctx, lat, x_e, x_o, &b_o, 1, 0, 0.5 / a, 1.0 / a)) != WD_OK) return st;
-        if (H == WD_PREC_DF64) {
-            if ((st = wd_convert_df_to_f64(ctx, (const float4 *)B.hx.v.p, dests[i]->d, 2 * nh)) != WD_OK) return st;
-        } else {
-            WD_CUDA(ctx, cudaMemcpyAsync(dests[i]->d, B.hx.v.p, 2 * nh * sizeof(double2), cudaMemcpyDeviceToDevice, ctx->stream));
-        }
-    }
-    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    const wd_precision H = prm->prec_reliable == WD_PREC_DF64 ? WD_PREC_DF64 : WD_PREC_F64;
+    const double delta = prm->delta > 0 && prm->delta < 1 ? prm->delta : 0.1;
+    BatchEngine eng(ctx, prm->prec, H, delta, 4, prm->max_iter);
+    wd_status st;
+    for (int i = 0; i < nsys; ++i)
+        if ((st = eng.add(i, lats[i], srcs[i]->d, dests[i]->d, masses[i], prm->tol)) != WD_OK) return st;
+    while (!eng.idle())
+        if ((st = eng.step(nullptr)) != WD_OK) return st;
+    const double secs = eng.solve_seconds;
     bool all = true;
-    for (int k = 0; k < nsys; ++k) {
-        const int i = sys_of_slot[k];
-        wd_solver_stats s{};
-        s.iterations = sb[k].iters;
-        s.reliable_updates = sb[k].updates;
-        s.residual = sb[k].true_res;
-        s.converged = sb[k].converged;
+    for (int i = 0; i < nsys; ++i) {
+        wd_solver_stats s = eng.results[i];
         s.seconds = secs;
         if (stats) {
             // FP64 true residual of each returned solution (a check, after the timed solve)
@@ -632,8 +765,312 @@ extern "C" wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice 
             if (st != WD_OK) return st;
             stats[i] = s;
         }
-        all = all && sb[k].converged;
+        all = all && s.converged;
     }
-    (void)graph_launches;
     return all ? WD_OK : WD_ERR_NOT_CONVERGED;
+}
+
+// ================================================================ serving
+//
+// A request: nsrc right-hand sides on one resident lattice, one mass and
+// tolerance.  Requests queue on submit; step() admits queued requests in
+// arrival order while the HBM budget (links + every admitted request's
+// fields and work buffers) and the slot count allow, advances all admitted
+// systems together by one engine quantum, and retires finished systems.
+// Requests admitted later join the running batch at the next quantum, so
+// work of different requests overlaps on the device.  In FP64 mode (the
+// plain drop-in), step() instead solves the oldest admitted system to the
+// end with the FP64 even-odd CG.
+
+namespace {
+uint64_t gen_mix(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ uint64_t dev_mix(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// complex Gaussian entry for reference index i (the host generator's counter
+// scheme), written at its device (structure-of-arrays) position
+__global__ void k_gen_source(uint64_t key, int Vh, double2 *out)
+{
+    const int64_t n = (int64_t)Vh * 24;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t h1 = dev_mix(key ^ (uint64_t)(2 * i)), h2 = dev_mix(key ^ (uint64_t)(2 * i + 1));
+        const double u1 = ((double)(h1 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+        const double u2 = ((double)(h2 >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+        const double r = sqrt(-2.0 * log(u1));
+        double sn, cs;
+        sincospi(2.0 * u2, &sn, &cs);
+        const int64_t site = i / 12, c = i % 12;
+        const int64_t par = site / Vh, s = site % Vh;
+        out[(par * 12 + c) * Vh + s] = make_double2(r * cs, r * sn);
+    }
+}
+}  // namespace
+
+struct wd_server {
+    wd_context *ctx = nullptr;
+    wd_server_config cfg{};
+    std::unique_ptr<BatchEngine> eng;
+    std::vector<wd_lattice *> lats;
+    double gauge_bytes = 0, req_bytes = 0;
+    struct Pending {
+        int64_t id;
+        int lat, nsrc;
+        std::vector<std::vector<double>> host;
+        std::vector<uint64_t> seeds;
+        double mass, tol;
+    };
+    std::deque<Pending> queue;
+    struct Req {
+        int lat = 0, nsrc = 0, remaining = 0;
+        std::vector<wd_field *> src, dest;
+        std::vector<wd_solver_stats> st;
+        double bytes = 0, mass = 0, tol = 0;
+        bool done = false;
+        std::chrono::steady_clock::time_point t_submit, t_done;
+    };
+    std::map<int64_t, Req> reqs;
+    std::map<int, std::pair<int64_t, int>> tag_req;
+    std::deque<int> fp64_todo;  // FP64 mode: tags waiting for their solve
+    int next_tag = 0, active_systems = 0;
+    int64_t next_id = 1;
+};
+
+static double field_bytes64(const wd_lattice *lat) { return (double)lat->volume * 12 * sizeof(double2); }
+
+static double request_bytes(const wd_server *sv, const wd_lattice *lat, int nsrc)
+{
+    double per = 2 * field_bytes64(lat);
+    if (sv->cfg.prec == WD_PREC_F64) per += 8 * 0.5 * field_bytes64(lat);  // the FP64 CG's half-lattice vectors
+    else per += (double)system_bytes(lat, sv->cfg.prec, sv->cfg.prec_reliable == WD_PREC_DF64 ? WD_PREC_DF64 : WD_PREC_F64);
+    return per * nsrc;
+}
+
+extern "C" void wd_server_config_default(wd_server_config *c)
+{
+    if (!c) return;
+    c->prec = WD_PREC_F32;
+    c->prec_reliable = WD_PREC_DF64;
+    c->hbm_budget_bytes = 150e9;
+    c->max_systems = 256;
+    c->max_iter = 5000;
+    c->delta = 0.1;
+}
+
+extern "C" wd_status wd_server_create(wd_context *ctx, const wd_server_config *cfg, wd_server **out)
+{
+    if (!ctx || !cfg || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if (cfg->prec != WD_PREC_F64 && cfg->prec != WD_PREC_F32 && cfg->prec != WD_PREC_F16)
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "server precision must be FP64 (plain) or FP32/FP16 (batched mixed)");
+    if (!(cfg->hbm_budget_bytes > 0) || cfg->max_systems < 1 || cfg->max_iter < 1)
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "bad server limits");
+    wd_server *sv = new wd_server();
+    sv->ctx = ctx;
+    sv->cfg = *cfg;
+    if (cfg->prec != WD_PREC_F64) {
+        const wd_precision H = cfg->prec_reliable == WD_PREC_DF64 ? WD_PREC_DF64 : WD_PREC_F64;
+        const double delta = cfg->delta > 0 && cfg->delta < 1 ? cfg->delta : 0.1;
+        sv->eng = std::make_unique<BatchEngine>(ctx, cfg->prec, H, delta, 4, cfg->max_iter);
+    }
+    *out = sv;
+    return WD_OK;
+}
+
+extern "C" void wd_server_destroy(wd_server *sv)
+{
+    if (!sv) return;
+    sv->eng.reset();
+    for (auto &kv : sv->reqs) {
+        for (wd_field *f : kv.second.src) wd_field_destroy(f);
+        for (wd_field *f : kv.second.dest) wd_field_destroy(f);
+    }
+    for (wd_lattice *l : sv->lats) wd_lattice_destroy(l);
+    delete sv;
+}
+
+extern "C" wd_status wd_server_add_lattice(wd_server *sv, const int dims[4], const double *const gauge[4], int *id)
+{
+    if (!sv || !id) return WD_ERR_BAD_ARG;
+    wd_lattice *lat = nullptr;
+    wd_status st = wd_lattice_create(sv->ctx, dims, gauge, &lat);
+    if (st != WD_OK) return st;
+    // derived link copies the server will use, built now so they count against the budget
+    double bytes = (double)lat->volume * 4 * 9 * sizeof(double2);
+    if (sv->cfg.prec != WD_PREC_F64) {
+        if ((st = wd_lattice_gauge_lp(sv->ctx, lat, sv->cfg.prec)) != WD_OK) return st;
+        bytes += (double)lat->volume * 4 * (sv->cfg.prec == WD_PREC_F16 ? 24 : 48);
+        if (sv->cfg.prec_reliable == WD_PREC_DF64) {
+            if ((st = wd_lattice_gauge_df(sv->ctx, lat)) != WD_OK) return st;
+            bytes += (double)lat->volume * 4 * 9 * sizeof(float4);
+        }
+    }
+    sv->gauge_bytes += bytes;
+    sv->lats.push_back(lat);
+    *id = (int)sv->lats.size() - 1;
+    return WD_OK;
+}
+
+extern "C" wd_status wd_server_submit(wd_server *sv, int lattice_id, int nsrc, const double *const *sources,
+                                      const uint64_t *seeds, double mass, double tol, int64_t *id)
+{
+    if (!sv || !id || nsrc < 1 || lattice_id < 0 || lattice_id >= (int)sv->lats.size() || !(tol > 0))
+        return sv ? wd_fail(sv->ctx, WD_ERR_BAD_ARG, "bad request") : WD_ERR_BAD_ARG;
+    if (!sources && !seeds) return wd_fail(sv->ctx, WD_ERR_BAD_ARG, "a request needs sources or seeds");
+    const wd_lattice *lat = sv->lats[lattice_id];
+    if (sv->gauge_bytes + request_bytes(sv, lat, nsrc) > sv->cfg.hbm_budget_bytes || nsrc > sv->cfg.max_systems)
+        return wd_fail(sv->ctx, WD_ERR_OOM, "request larger than the server's HBM budget or slot count");
+    wd_server::Pending p;
+    p.id = sv->next_id++;
+    p.lat = lattice_id, p.nsrc = nsrc, p.mass = mass, p.tol = tol;
+    const size_t n = (size_t)lat->volume * 24;
+    for (int k = 0; k < nsrc; ++k) {
+        if (sources) p.host.emplace_back(sources[k], sources[k] + n);
+        else p.seeds.push_back(seeds[k]);
+    }
+    wd_server::Req r;
+    r.lat = lattice_id, r.nsrc = nsrc, r.remaining = nsrc, r.mass = mass, r.tol = tol;
+    r.st.resize(nsrc);
+    r.t_submit = std::chrono::steady_clock::now();
+    sv->reqs[p.id] = std::move(r);
+    *id = p.id;
+    sv->queue.push_back(std::move(p));
+    return WD_OK;
+}
+
+// upload or generate one source into an FP64 field (unit L2 norm for generated ones)
+static wd_status server_source(wd_server *sv, const wd_server::Pending &p, int k, wd_field *f)
+{
+    wd_context *ctx = sv->ctx;
+    if (!p.host.empty()) return wd_field_upload(ctx, f, p.host[k].data());
+    const int Vh = f->lat->g.Vh;
+    k_gen_source<<<152 * 8, 256, 0, ctx->stream>>>(gen_mix(p.seeds[k] ^ 0xA5A5A5A5ull), Vh, f->d);
+    WD_LAUNCHED(ctx);
+    const int64_t n = f->lat->volume * 12;
+    wd_status st = wd_red_norm2(ctx, f->d, n, 0);
+    if (st != WD_OK) return st;
+    double2 v;
+    if ((st = wd_red_fetch(ctx, 1, &v)) != WD_OK) return st;
+    return wd_blas_scale(ctx, v.x > 0 ? 1.0 / std::sqrt(v.x) : 1.0, f->d, f->d, n);
+}
+
+static wd_status server_admit(wd_server *sv)
+{
+    wd_status st;
+    while (!sv->queue.empty()) {
+        wd_server::Pending &p = sv->queue.front();
+        const wd_lattice *lat = sv->lats[p.lat];
+        const double bytes = request_bytes(sv, lat, p.nsrc);
+        if (sv->gauge_bytes + sv->req_bytes + bytes > sv->cfg.hbm_budget_bytes) break;
+        if (sv->active_systems > 0 && sv->active_systems + p.nsrc > sv->cfg.max_systems) break;
+        wd_server::Req &r = sv->reqs[p.id];
+        r.bytes = bytes;
+        sv->req_bytes += bytes;
+        for (int k = 0; k < p.nsrc; ++k) {
+            wd_field *fs = nullptr, *fd = nullptr;
+            if ((st = wd_field_create(sv->ctx, lat, &fs)) != WD_OK) return st;
+            r.src.push_back(fs);
+            if ((st = wd_field_create(sv->ctx, lat, &fd)) != WD_OK) return st;
+            r.dest.push_back(fd);
+            if ((st = server_source(sv, p, k, fs)) != WD_OK) return st;
+            const int tag = sv->next_tag++;
+            sv->tag_req[tag] = {p.id, k};
+            sv->active_systems++;
+            if (sv->eng) {
+                if ((st = sv->eng->add(tag, lat, fs->d, fd->d, p.mass, p.tol)) != WD_OK) return st;
+            } else {
+                sv->fp64_todo.push_back(tag);
+            }
+        }
+        sv->queue.pop_front();
+    }
+    return WD_OK;
+}
+
+static void server_retire(wd_server *sv, int tag, const wd_solver_stats &s, int *completed)
+{
+    auto tr = sv->tag_req.find(tag);
+    if (tr == sv->tag_req.end()) return;
+    wd_server::Req &r = sv->reqs[tr->second.first];
+    r.st[tr->second.second] = s;
+    sv->tag_req.erase(tr);
+    sv->active_systems--;
+    if (--r.remaining == 0) {
+        r.done = true;
+        r.t_done = std::chrono::steady_clock::now();
+        for (wd_field *f : r.src) wd_field_destroy(f);
+        r.src.clear();
+        ++*completed;
+    }
+}
+
+extern "C" wd_status wd_server_step(wd_server *sv, int *completed)
+{
+    if (!sv) return WD_ERR_BAD_ARG;
+    int done = 0;
+    wd_status st = server_admit(sv);
+    if (st != WD_OK) return st;
+    std::vector<int> fin;
+    if (sv->eng) {
+        sv->eng->take_retired(&fin);  // systems already solved at admission
+        if ((st = sv->eng->step(nullptr)) != WD_OK) return st;
+        sv->eng->take_retired(&fin);
+        for (int tag : fin) server_retire(sv, tag, sv->eng->results[tag], &done);
+        for (int tag : fin) sv->eng->results.erase(tag);
+    } else if (!sv->fp64_todo.empty()) {
+        const int tag = sv->fp64_todo.front();
+        sv->fp64_todo.pop_front();
+        const auto &tr = sv->tag_req[tag];
+        wd_server::Req &r = sv->reqs[tr.first];
+        wd_solver_params p;
+        wd_solver_params_default(&p);
+        p.kind = WD_SOLVER_CG_EO;
+        p.mass = r.mass, p.tol = r.tol, p.max_iter = sv->cfg.max_iter, p.prec = WD_PREC_F64;
+        wd_solver_stats s{};
+        st = wd_solve(sv->ctx, sv->lats[r.lat], r.src[tr.second], r.dest[tr.second], &p, &s);
+        if (st != WD_OK && st != WD_ERR_NOT_CONVERGED) return st;
+        server_retire(sv, tag, s, &done);
+    }
+    if (completed) *completed = done;
+    return WD_OK;
+}
+
+extern "C" wd_status wd_server_poll(wd_server *sv, int64_t id, int *done, double *const *solutions,
+                                    wd_solver_stats *stats, double *latency_s)
+{
+    if (!sv || !done) return WD_ERR_BAD_ARG;
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return wd_fail(sv->ctx, WD_ERR_BAD_ARG, "unknown or already collected request");
+    wd_server::Req &r = it->second;
+    *done = r.done ? 1 : 0;
+    if (!r.done) return WD_OK;
+    wd_status st = WD_OK;
+    for (int k = 0; k < r.nsrc; ++k) {
+        if (solutions && solutions[k] && st == WD_OK) st = wd_field_download(sv->ctx, r.dest[k], solutions[k]);
+        if (stats) stats[k] = r.st[k];
+    }
+    if (latency_s) *latency_s = std::chrono::duration<double>(r.t_done - r.t_submit).count();
+    for (wd_field *f : r.dest) wd_field_destroy(f);
+    sv->req_bytes -= r.bytes;
+    sv->reqs.erase(it);
+    return st;
+}
+
+extern "C" wd_status wd_server_status(const wd_server *sv, int *queued, int *active_systems, double *bytes_in_use)
+{
+    if (!sv) return WD_ERR_BAD_ARG;
+    if (queued) *queued = (int)sv->queue.size();
+    if (active_systems) *active_systems = sv->active_systems;
+    if (bytes_in_use) *bytes_in_use = sv->gauge_bytes + sv->req_bytes;
+    return WD_OK;
 }

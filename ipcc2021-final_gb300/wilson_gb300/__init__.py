@@ -38,6 +38,11 @@ class SolverParams(C.Structure):
                 ("prec_reliable", C.c_int)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("prec", C.c_int), ("prec_reliable", C.c_int), ("hbm_budget_bytes", C.c_double),
+                ("max_systems", C.c_int), ("max_iter", C.c_int), ("delta", C.c_double)]
+
+
 class SolverStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("reliable_updates", C.c_int), ("residual", C.c_double),
                 ("true_residual", C.c_double), ("seconds", C.c_double), ("converged", C.c_int)]
@@ -87,6 +92,16 @@ def _load() -> C.CDLL:
         "wd_host_dslash_offd": (C.c_int, [vp, ip, d4, vp, vp, C.c_int, C.c_int]),
         "wd_host_dslash_full": (C.c_int, [vp, ip, d4, vp, vp, C.c_double, C.c_int]),
         "wd_host_cg": (C.c_int, [vp, ip, d4, vp, vp, C.POINTER(SolverParams), C.POINTER(SolverStats)]),
+        "wd_server_config_default": (None, [C.POINTER(ServerConfig)]),
+        "wd_server_create": (C.c_int, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
+        "wd_server_destroy": (None, [vp]),
+        "wd_server_add_lattice": (C.c_int, [vp, ip, d4, ip]),
+        "wd_server_submit": (C.c_int, [vp, C.c_int, C.c_int, C.POINTER(vp), C.POINTER(C.c_uint64), C.c_double,
+                                       C.c_double, C.POINTER(C.c_int64)]),
+        "wd_server_step": (C.c_int, [vp, ip]),
+        "wd_server_poll": (C.c_int, [vp, C.c_int64, ip, C.POINTER(vp), C.POINTER(SolverStats),
+                                     C.POINTER(C.c_double)]),
+        "wd_server_status": (C.c_int, [vp, ip, ip, dp]),
         "wd_gen_gauge": (C.c_int, [ip, C.c_uint64, C.c_double, d4]),
         "wd_gen_source": (C.c_int, [ip, C.c_uint64, vp]),
     }
@@ -351,3 +366,78 @@ def solver_params(kind: int = CG_EO, mass: float = 0.1, tol: float = 1e-10, max_
     p.use_initial_guess = int(use_initial_guess)
     p.prec_reliable = prec_reliable
     return p
+
+
+class Server:
+    """Continuous-batching solve server on one context (see wd_server_* in the C header)."""
+
+    def __init__(self, ctx: Context, prec: int = F32, prec_reliable: int = DF64, hbm_budget_bytes: float = 150e9,
+                 max_systems: int = 256, max_iter: int = 5000, delta: float = 0.1):
+        self.ctx = ctx
+        cfg = ServerConfig()
+        lib.wd_server_config_default(C.byref(cfg))
+        cfg.prec, cfg.prec_reliable, cfg.hbm_budget_bytes = prec, prec_reliable, hbm_budget_bytes
+        cfg.max_systems, cfg.max_iter, cfg.delta = max_systems, max_iter, delta
+        h = C.c_void_p()
+        ctx.check(lib.wd_server_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h
+        self.dims = {}
+        self.nsrc = {}
+
+    def close(self) -> None:
+        if self.handle:
+            lib.wd_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_lattice(self, dims, gauge) -> int:
+        i = C.c_int()
+        self.ctx.check(lib.wd_server_add_lattice(self.handle, _dims(dims), _gauge_ptrs(gauge), C.byref(i)))
+        self.dims[i.value] = tuple(int(v) for v in dims)
+        return i.value
+
+    def submit(self, lattice_id: int, nsrc: int, mass: float, tol: float, sources=None, seeds=None) -> int:
+        rid = C.c_int64()
+        src_arr = None
+        seed_arr = None
+        if sources is not None:
+            src_arr = (C.c_void_p * nsrc)(*[_ptr(a).value for a in sources])
+        else:
+            seed_arr = (C.c_uint64 * nsrc)(*[int(v) for v in seeds])
+        self.ctx.check(lib.wd_server_submit(self.handle, lattice_id, nsrc, src_arr, seed_arr, float(mass), float(tol),
+                                            C.byref(rid)))
+        self.nsrc[rid.value] = (lattice_id, nsrc)
+        return rid.value
+
+    def step(self) -> int:
+        n = C.c_int()
+        self.ctx.check(lib.wd_server_step(self.handle, C.byref(n)))
+        return n.value
+
+    def poll(self, rid: int, want_solutions: bool = False):
+        """(done, solutions or None, stats list, latency seconds); collected requests are released."""
+        lat, nsrc = self.nsrc[rid]
+        done = C.c_int()
+        stats = (SolverStats * nsrc)()
+        lat_s = C.c_double()
+        sols = None
+        sol_ptrs = None
+        if want_solutions:
+            V = volume(self.dims[lat])
+            sols = [np.empty(V * 12, np.complex128) for _ in range(nsrc)]
+            sol_ptrs = (C.c_void_p * nsrc)(*[_ptr(a).value for a in sols])
+        self.ctx.check(lib.wd_server_poll(self.handle, rid, C.byref(done), sol_ptrs, stats, C.byref(lat_s)))
+        if not done.value:
+            return False, None, None, None
+        del self.nsrc[rid]
+        return True, sols, list(stats), lat_s.value
+
+    def status(self):
+        q, a, b = C.c_int(), C.c_int(), C.c_double()
+        self.ctx.check(lib.wd_server_status(self.handle, C.byref(q), C.byref(a), C.byref(b)))
+        return q.value, a.value, b.value
