@@ -260,6 +260,77 @@ def batch_bench(wd, ctx) -> dict:
     return out
 
 
+SERVE_SIZES = [((8, 8, 8, 16), 0.4), ((16, 16, 16, 32), 0.3), ((24, 24, 24, 48), 0.2), ((32, 32, 32, 64), 0.1)]
+
+
+def serve_workload(n: int, seed: int = 7):
+    """n requests: lattice size from the configured mix, one of the two resident
+    gauge fields of that size, mass U[0.02, 0.2], tol from {1e-8, 1e-10},
+    1-12 seeded Gaussian sources."""
+    rng = np.random.default_rng(seed)
+    probs = [p for _, p in SERVE_SIZES]
+    reqs = []
+    for i in range(n):
+        c = int(rng.choice(len(SERVE_SIZES), p=probs))
+        reqs.append({"size": c, "gauge": 2 * c + int(rng.integers(2)), "mass": float(rng.uniform(0.02, 0.2)),
+                     "tol": float(rng.choice([1e-8, 1e-10])), "nsrc": int(rng.integers(1, 13)),
+                     "seeds": [int(v) for v in rng.integers(1, 2**62, size=13)]})
+    return reqs
+
+
+def serve_run(wd, ctx, reqs, rate: float, prec: int, budget: float = 150e9, seed: int = 11) -> dict:
+    """Poisson arrivals at `rate` requests/s into a server; returns latency
+    percentiles and throughput.  Latency = completion - arrival."""
+    import time as _t
+    sv = wd.Server(ctx, prec=prec, prec_reliable=wd.DF64, hbm_budget_bytes=budget)
+    gids = []
+    for c, (dims, _) in enumerate(SERVE_SIZES):
+        for k in range(2):
+            gids.append(sv.add_lattice(dims, wd.gen_gauge(dims, 500 + 2 * c + k, EPS)))
+    arrivals = np.cumsum(np.random.default_rng(seed).exponential(1.0 / rate, size=len(reqs)))
+    t0 = _t.perf_counter()
+    pending, lat, solves, worst = {}, [], 0, 0.0
+    i = 0
+    while i < len(reqs) or pending:
+        now = _t.perf_counter() - t0
+        while i < len(reqs) and arrivals[i] <= now:
+            r = reqs[i]
+            rid = sv.submit(gids[r["gauge"]], r["nsrc"], r["mass"], r["tol"], seeds=r["seeds"][:r["nsrc"]])
+            pending[rid] = (arrivals[i], r)
+            i += 1
+        q, active, _ = sv.status()
+        if active or q:
+            sv.step()
+        elif i < len(reqs):
+            _t.sleep(max(0.0, arrivals[i] - (_t.perf_counter() - t0)))
+            continue
+        done_now = _t.perf_counter() - t0
+        for rid in list(pending):
+            done, _, stats, _ = sv.poll(rid)
+            if done:
+                arr, r = pending.pop(rid)
+                lat.append(done_now - arr)
+                solves += r["nsrc"]
+                worst = max(worst, max(st.residual / r["tol"] for st in stats))
+                assert all(st.converged for st in stats)
+    wall = _t.perf_counter() - t0
+    sv.close()
+    lat = np.array(lat)
+    return {"rate_req_per_s": rate, "requests": len(reqs), "solves": solves, "wall_s": wall,
+            "solves_per_s": solves / wall, "requests_per_s": len(reqs) / wall,
+            "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+            "max_residual_over_tol": worst}
+
+
+def serve_bench(wd, ctx, n: int, rates_mixed, rates_f64) -> dict:
+    reqs = serve_workload(n)
+    out = {"workload": f"{n} Poisson-arrival requests, sizes {{8^3x16:.4, 16^3x32:.3, 24^3x48:.2, 32^3x64:.1}}, "
+                       "mass U[0.02,0.2], tol {1e-8,1e-10}, 1-12 sources, 8 resident gauge fields, 150 GB budget",
+           "mixed_batched_f32": [serve_run(wd, ctx, reqs, r, wd.F32) for r in rates_mixed],
+           "plain_f64": [serve_run(wd, ctx, reqs, r, wd.F64) for r in rates_f64]}
+    return out
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -407,6 +478,8 @@ def run_ours(args) -> None:
                               **solver_bench(wd, ctx, lat, src, MASS)}
         if not args.no_batch:
             line["batch"] = batch_bench(wd, ctx)
+        if args.serve_requests > 0:
+            line["serving"] = serve_bench(wd, ctx, args.serve_requests, args.serve_rates, args.serve_rates_f64)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_port(gauge, src, dims)
         print(json.dumps(line), flush=True)
@@ -426,6 +499,12 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true", help="skip the CG solves/s measurements")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurements")
+    ap.add_argument("--serve-requests", type=int, default=24,
+                    help="requests per serving run (the configured workload has 2000; 0 skips serving)")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[8.0],
+                    help="arrival rates (requests/s) for the batched mixed-precision server")
+    ap.add_argument("--serve-rates-f64", type=float, nargs="*", default=[3.0],
+                    help="arrival rates (requests/s) for the plain FP64 server")
     ap.add_argument("--dims", type=int, nargs=4, default=list(DIMS),
                     help="lattice extents (default 32 32 32 64, the benchmark configuration)")
     args = ap.parse_args()
