@@ -331,6 +331,24 @@ def serve_bench(wd, ctx, n: int, rates_mixed, rates_f64) -> dict:
     return out
 
 
+def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
+    """The slowest rank's time: replicas run independent lattices, and the
+    job is done when the last one is."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: float, seconds_max: float, world: int) -> float:
+    """Whole-job throughput of `world` replicas: all ranks' units over the max time."""
+    return world * units_per_rank / seconds_max
+
+
 def run_reference(args) -> None:
     rank, world, _ = dist_env()
     if rank != 0:
@@ -413,12 +431,8 @@ def run_ours(args) -> None:
     launches = ctx.launches - launches0
     clk = clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = world * bps * vh / (t_max * 1e-3) / 1e9
+    t_max = max_over_ranks(ms, world)
+    value = replica_throughput(bps * vh, t_max * 1e-3, world) / 1e9
 
     # e2e through the reference-facing entry point, pinned host buffers
     e2e = None
@@ -433,12 +447,8 @@ def run_ours(args) -> None:
         for _ in range(n_e2e):
             ctx.check(wd.lib.wd_host_dslash_offd(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
                                                  wd._ptr(h_src), wd._ptr(h_dst), 0, 0))
-        e2e_s = (time.perf_counter() - t0) / n_e2e
-        if world > 1:
-            t = torch.tensor([e2e_s], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * BYTES_PER_SITE_F64 * vh / e2e_s / 1e9, "unit": "GB/s",
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e, world)
+        e2e = {"value": replica_throughput(BYTES_PER_SITE_F64 * vh, e2e_s, world) / 1e9, "unit": "GB/s",
                "h2d_bytes_per_step": int(src.nbytes), "d2h_bytes_per_step": int(src.nbytes), "steps": n_e2e,
                "path": "wd_host_dslash_offd (DslashoffdNew), pinned host buffers, links resident"}
 
