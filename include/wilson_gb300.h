@@ -165,6 +165,18 @@ wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice *const *lat
                          wd_field *const *dests, const double *masses, const wd_solver_params *params,
                          wd_solver_stats *stats);
 
+/* ---- propagator and pion correlator (the reference prototype's refs/python/main.py:50-66,
+ *      refs/python/contraction.py:26-45, in this library's gamma basis) ---- */
+/* f = unit point source at site x (global coordinates), spin s, colour c (FP64 field). */
+wd_status wd_point_source(wd_context *ctx, wd_field *f, const int x[4], int spin, int colour);
+/* The 12 columns props[s*3+c] = M^-1 point_source(x_src, s, c), solved with params (a mixed
+ * prec batches all 12 as right-hand sides of one lattice); stats may be NULL. */
+wd_status wd_propagator(wd_context *ctx, const wd_lattice *lat, const int x_src[4], const wd_solver_params *params,
+                        wd_field *const props[12], wd_solver_stats stats[12]);
+/* Pion two-point function ct[t] = sum over the sites of time slice t (absolute t) of
+ * sum_{columns} |psi|^2 (gamma5-hermiticity), t = 0..Lt-1, deterministic order. */
+wd_status wd_pion_correlator(wd_context *ctx, const wd_lattice *lat, const wd_field *const props[12], double *ct);
+
 /* ---- serving: continuous batching of solve requests (no counterpart in the reference) ---- */
 typedef struct wd_server wd_server;
 typedef struct wd_server_config {

@@ -92,6 +92,9 @@ def _load() -> C.CDLL:
         "wd_host_dslash_offd": (C.c_int, [vp, ip, d4, vp, vp, C.c_int, C.c_int]),
         "wd_host_dslash_full": (C.c_int, [vp, ip, d4, vp, vp, C.c_double, C.c_int]),
         "wd_host_cg": (C.c_int, [vp, ip, d4, vp, vp, C.POINTER(SolverParams), C.POINTER(SolverStats)]),
+        "wd_point_source": (C.c_int, [vp, vp, ip, C.c_int, C.c_int]),
+        "wd_propagator": (C.c_int, [vp, vp, ip, C.POINTER(SolverParams), C.POINTER(vp), C.POINTER(SolverStats)]),
+        "wd_pion_correlator": (C.c_int, [vp, vp, C.POINTER(vp), dp]),
         "wd_server_config_default": (None, [C.POINTER(ServerConfig)]),
         "wd_server_create": (C.c_int, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
         "wd_server_destroy": (None, [vp]),
@@ -301,6 +304,22 @@ class Lattice:
         if not (allow_unconverged and st == NOT_CONVERGED):
             self.ctx.check(st)
         return stats
+
+    def propagator(self, x_src, params: SolverParams):
+        """12 FP64 fields M^-1 (point source at x_src, spin s, colour c), index s*3+c, and their stats."""
+        props = [self.field() for _ in range(12)]
+        arr = (C.c_void_p * 12)(*[f.handle.value for f in props])
+        stats = (SolverStats * 12)()
+        self.ctx.check(lib.wd_propagator(self.ctx.handle, self.handle, (C.c_int * 4)(*x_src), C.byref(params), arr,
+                                         stats))
+        return props, list(stats)
+
+    def pion_correlator(self, props) -> np.ndarray:
+        ct = np.zeros(self.dims[3], np.float64)
+        arr = (C.c_void_p * 12)(*[f.handle.value for f in props])
+        self.ctx.check(lib.wd_pion_correlator(self.ctx.handle, self.handle, arr,
+                                              ct.ctypes.data_as(C.POINTER(C.c_double))))
+        return ct
 
     def check(self, b: "Field", x: "Field", mass: float) -> np.ndarray:
         out = np.zeros(12, np.float64)

@@ -93,3 +93,40 @@ def test_command_line_driver_matches_oracle(wd, oracle):
     assert got_res < 1e-6 * chk[0] and chk[10] < 1e-6 * chk[0]
     for line in ("Source and Gauge, time:", "CG invert, time:", "Total time:", "|M^dagger M x - Mdb| ="):
         assert line in out
+
+
+def _write_gauge_file(path, gauge, dims, header=b"", trailer=b""):
+    """Big-endian doubles, [site lex][mu][row][col][re, im] (src/load_gauge.cpp:110-161)."""
+    Lx, Ly, Lz, Lt = dims
+    V = Lx * Ly * Lz * Lt
+    eo_of_lex = np.empty(V, np.int64)
+    for lex in range(V):
+        x, y, z, t = lex % Lx, (lex // Lx) % Ly, (lex // (Lx * Ly)) % Lz, lex // (Lx * Ly * Lz)
+        eo_of_lex[lex] = lex // 2 + ((x + y + z + t) & 1) * (V // 2)
+    data = np.stack([g.reshape(V, 9)[eo_of_lex] for g in gauge], axis=1)
+    with open(path, "wb") as f:
+        f.write(header)
+        f.write(data.view(np.float64).astype(">f8").tobytes())
+        f.write(trailer)
+
+
+@pytest.mark.parametrize("framing", ["plain", "lime"])
+def test_driver_reads_gauge_files(wd, oracle, golden4, tmp_path, framing):
+    b = _build_module()
+    g = golden4
+    path = tmp_path / "conf.dat"
+    if framing == "plain":
+        _write_gauge_file(path, g["gauge"], g["dims"])
+    else:
+        _write_gauge_file(path, g["gauge"], g["dims"], header=b"L" * 1000, trailer=b"T" * 280)
+    dims, seed, mass = g["dims"], 5, 0.1
+    r = subprocess.run([str(b.MAIN_BIN), str(mass), str(path), *map(str, dims), *map(str, dims), str(seed)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    src, x0 = oracle.main_inputs(dims, seed)
+    x, iters, rsd = oracle.cg_ref(src, g["gauge"], dims, mass, 500, 1e-9, x0)
+    m = re.search(r"CG: (\d+) iterations", r.stdout)
+    assert m and abs(int(m.group(1)) - iters) <= 1, r.stdout
+    chk = oracle.check(src, x, g["gauge"], dims, mass)
+    got = re.search(r"\(Mx, Mx\) = \(([0-9.eE+-]+),", r.stdout)
+    assert abs(float(got.group(1)) - chk[6]) < 1e-5 * chk[6]   # the report prints 6 significant digits
