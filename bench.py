@@ -156,6 +156,33 @@ def cpu_baseline_port(gauge, src, dims, seconds: float = 12.0) -> dict:
                       f"{dt * 1e3:.1f} ms each, C restatement with OpenMP over sites"}
 
 
+def dslash_variants(wd, ctx, lat, src, stream, steps: int, vh: int, peak: float) -> dict:
+    """D_eo in the other storage formats on the same lattice (CUDA events)."""
+    import torch
+
+    out = {}
+    for name, prec in (("df64", wd.DF64), ("f32", wd.F32), ("f16", wd.F16)):
+        fi, fo = lat.field(src, prec=prec), lat.field(prec=prec)
+        for _ in range(5):
+            lat.dslash_eo(fi, fo, 0, 0, prec)
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            lat.dslash_eo(fi, fo, 0, 0, prec)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        gbs = BYTES_PER_SITE[name] * vh / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "gbs": gbs, "frac_of_hbm": gbs / peak, "bytes_per_site": BYTES_PER_SITE[name],
+                     "gflops": FLOPS_PER_SITE * vh / (ms * 1e-3) / 1e9}
+        fi.close()
+        fo.close()
+    out["note"] = ("df64: FP64-class results (<=1e-13 rel. L2 vs the FP64 oracle) from float pairs on the "
+                   "FP32 pipe; f32/f16: the mixed solvers' inner operators (12-real links)")
+    return out
+
+
 def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10) -> dict:
     """One solve per arithmetic on the resident lattice: solves/s, iterations,
     FP64 true residual, and the relative difference to the FP64 solution."""
@@ -482,6 +509,10 @@ def run_ours(args) -> None:
             "gpu_launches": launches,
             "clocks": clk,
         }
+        if args.prec == "f64":
+            line["dslash_other_storage"] = dslash_variants(wd, ctx, lat, src, stream, min(args.steps, 300), vh, peak)
+        line["autotune"] = [{"kernel": k, "half_volume": v, "variant": var, "ms": ms}
+                            for _, k, v, var, ms in wd.tune_report()]
         if not args.no_solver:
             line["solver"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, dims))}, "
                                           f"mass {MASS}, seed 2",

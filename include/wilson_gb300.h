@@ -257,6 +257,14 @@ wd_status wd_host_dot(wd_context *ctx, int64_t n, const double *a, const double 
 wd_status wd_host_check(wd_context *ctx, const int dims[4], const double *const gauge[4], const double *b,
                         const double *x, double mass, double out[12]);
 
+/* Launch-shape autotuner: the first call of a hopping kernel for a lattice
+ * half-volume times its launch variants and keeps the fastest.  The report
+ * lists "device kernel Vh variant ms" lines; returns its length.  Tuning
+ * can be switched off (variant 0 everywhere); WD_TUNE=0 does the same and
+ * WD_TUNE_CACHE=<file> persists decisions. */
+int wd_tune_report(char *buf, int len);
+void wd_tune_enable(int on);
+
 /* ---- seeded synthetic inputs (host, deterministic) ---------------------- */
 /* Gauge links U = exp(i eps H) re-unitarised to SU(3), H Gaussian traceless
  * hermitian; written in the reference layout (4 arrays of V*9 complex). */

@@ -17,12 +17,13 @@
 #include "wd_hop.cuh"
 #include "wd_df.cuh"
 #include "wd_kernels.h"
+#include <type_traits>
+#include "wd_tune.h"
 
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kSitesPerWarp = 10;
-constexpr int kSplitWarps = 4;
 
 struct SplitDF {
     WdGeom g;
@@ -84,13 +85,13 @@ __device__ __forceinline__ void split_dir(const SplitDF &p, int s, const WdSite 
     wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
 }
 
-template <bool DAG>
-__global__ void __launch_bounds__(32 * kSplitWarps) k_hop_df_split(const SplitDF p)
+template <bool DAG, int WARPS, int MINB>
+__global__ void __launch_bounds__(32 * WARPS, MINB) k_hop_df_split(const SplitDF p)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int cq = lane / kSitesPerWarp;          // 0..2, 3 for the two idle lanes
     const int ls = lane - cq * kSitesPerWarp;     // site within the warp
-    const int s_raw = (blockIdx.x * kSplitWarps + warp) * kSitesPerWarp + ls;
+    const int s_raw = (blockIdx.x * WARPS + warp) * kSitesPerWarp + ls;
     const bool on = cq < 3 && s_raw < p.g.Vh;
     const int col = cq < 3 ? cq : 0;
     const int s = on ? s_raw : 0;                 // idle lanes compute on site 0 and store nothing
@@ -157,12 +158,24 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
     p.out = out_block;
     p.alpha = df_split(alpha);
     p.beta = df_split(beta);
-    const int sites_per_block = kSitesPerWarp * kSplitWarps;
-    const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
-    if (dag) k_hop_df_split<true><<<blocks, 32 * kSplitWarps, 0, ctx->stream>>>(p);
-    else k_hop_df_split<false><<<blocks, 32 * kSplitWarps, 0, ctx->stream>>>(p);
-    WD_LAUNCHED(ctx);
-    return WD_OK;
+    auto run = [&](auto warps, auto minb) -> wd_status {
+        constexpr int W = decltype(warps)::value, M = decltype(minb)::value;
+        const int sites_per_block = kSitesPerWarp * W;
+        const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
+        if (dag) k_hop_df_split<true, W, M><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        else k_hop_df_split<false, W, M><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
+    using I = std::integral_constant<int, 0>;
+    // variants: 4 warps/block; 2; 8; 4 warps with 6 blocks per SM (80 registers)
+    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 4, [&](int v) -> wd_status {
+        if (v == 1) return run(std::integral_constant<int, 2>(), std::integral_constant<int, 1>());
+        if (v == 2) return run(std::integral_constant<int, 8>(), std::integral_constant<int, 1>());
+        if (v == 3) return run(std::integral_constant<int, 4>(), std::integral_constant<int, 6>());
+        (void)I();
+        return run(std::integral_constant<int, 4>(), std::integral_constant<int, 1>());
+    });
 }
 
 wd_status wd_convert_f64_to_df(wd_context *ctx, const double2 *in, float4 *out, int64_t n)

@@ -8,12 +8,15 @@
 // double-float variant that moves the arithmetic onto the FP32 pipe.
 #include "wd_hop.cuh"
 #include "wd_kernels.h"
+#include <type_traits>
+#include "wd_tune.h"
 
 namespace {
 
+template <int THREADS>
 struct HopF64 {
     using C = double2;
-    static constexpr int kThreads = 128;
+    static constexpr int kThreads = THREADS;
     WdGeom g;
     int cb;
     const double2 *__restrict__ in;     // parity 1-cb block [12][Vh]
@@ -52,19 +55,27 @@ wd_status wd_hop_f64(wd_context *ctx, const wd_lattice *lat, const double2 *in_b
                      double2 *out_block, const double2 *x_block, int cb, int dag, double alpha,
                      double beta)
 {
-    HopF64 p;
-    p.g = lat->g;
-    p.cb = cb;
-    p.in = in_block;
-    p.gauge = lat->gauge;
-    p.x = x_block;
-    p.out = out_block;
-    p.alpha = alpha;
-    p.beta = beta;
-    const int threads = HopF64::kThreads;
-    const int blocks = (lat->g.Vh + threads - 1) / threads;
-    if (dag) wd_hop_kernel<true><<<blocks, threads, 0, ctx->stream>>>(p);
-    else wd_hop_kernel<false><<<blocks, threads, 0, ctx->stream>>>(p);
-    WD_LAUNCHED(ctx);
-    return WD_OK;
+    auto run = [&](auto tag) -> wd_status {
+        using P = HopF64<decltype(tag)::value>;
+        P p;
+        p.g = lat->g;
+        p.cb = cb;
+        p.in = in_block;
+        p.gauge = lat->gauge;
+        p.x = x_block;
+        p.out = out_block;
+        p.alpha = alpha;
+        p.beta = beta;
+        const int blocks = (lat->g.Vh + P::kThreads - 1) / P::kThreads;
+        if (dag) wd_hop_kernel<true><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+        else wd_hop_kernel<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
+    // variants: 128, 64, 256 threads per block
+    return wd_tune_launch(ctx, "hop_f64", lat->g.Vh, 3, [&](int v) -> wd_status {
+        if (v == 1) return run(std::integral_constant<int, 64>());
+        if (v == 2) return run(std::integral_constant<int, 256>());
+        return run(std::integral_constant<int, 128>());
+    });
 }

@@ -9,13 +9,15 @@
 #include "wd_hop.cuh"
 #include "wd_lp.cuh"
 #include "wd_kernels.h"
+#include <type_traits>
+#include "wd_tune.h"
 
 namespace {
 
-template <class Sp, class Lk>
+template <class Sp, class Lk, int THREADS = 128>
 struct HopLP {
     using C = float2;
-    static constexpr int kThreads = 128;
+    static constexpr int kThreads = THREADS;
     WdGeom g;
     int cb;
     Sp in, out, x;
@@ -143,6 +145,23 @@ wd_status launch_hop(wd_context *ctx, const P &p, int dag)
     return WD_OK;
 }
 
+// the same operands launched with 128, 64 or 256 threads per block (tuned)
+template <class Sp, class Lk>
+wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p, int dag)
+{
+    return wd_tune_launch(ctx, name, p.g.Vh, 3, [&](int v) -> wd_status {
+        auto with = [&](auto tag) {
+            HopLP<Sp, Lk, decltype(tag)::value> q;
+            q.g = p.g, q.cb = p.cb, q.in = p.in, q.out = p.out, q.x = p.x, q.link = p.link;
+            q.has_x = p.has_x, q.alpha = p.alpha, q.beta = p.beta;
+            return launch_hop(ctx, q, dag);
+        };
+        if (v == 1) return with(std::integral_constant<int, 64>());
+        if (v == 2) return with(std::integral_constant<int, 256>());
+        return with(std::integral_constant<int, 128>());
+    });
+}
+
 }  // namespace
 
 wd_status wd_lattice_gauge_lp(wd_context *ctx, const wd_lattice *lat_c, wd_precision prec)
@@ -179,7 +198,7 @@ wd_status wd_hop_f32(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out
     p.link = LinkF32{(const float4 *)lat->gauge_f32, lat->g.Vh};
     p.alpha = (float)alpha;
     p.beta = (float)beta;
-    return launch_hop(ctx, p, dag);
+    return launch_tuned(ctx, "hop_f32", p, dag);
 }
 
 wd_status wd_hop_f16(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
@@ -198,7 +217,7 @@ wd_status wd_hop_f16(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out
     p.link = LinkF16{a, (const uint2 *)(a + (size_t)8 * lat->g.Vh), lat->g.Vh};
     p.alpha = (float)alpha;
     p.beta = (float)beta;
-    return launch_hop(ctx, p, dag);
+    return launch_tuned(ctx, "hop_f16", p, dag);
 }
 
 wd_status wd_lp_from_f64(wd_context *ctx, int Vh, const double2 *in, WdVec out)

@@ -105,6 +105,8 @@ def _load() -> C.CDLL:
         "wd_server_poll": (C.c_int, [vp, C.c_int64, ip, C.POINTER(vp), C.POINTER(SolverStats),
                                      C.POINTER(C.c_double)]),
         "wd_server_status": (C.c_int, [vp, ip, ip, dp]),
+        "wd_tune_report": (C.c_int, [C.c_char_p, C.c_int]),
+        "wd_tune_enable": (None, [C.c_int]),
         "wd_gen_gauge": (C.c_int, [ip, C.c_uint64, C.c_double, d4]),
         "wd_gen_source": (C.c_int, [ip, C.c_uint64, vp]),
     }
@@ -142,6 +144,17 @@ def _gauge_ptrs(gauge) -> C.Array:
 
 def volume(dims) -> int:
     return int(np.prod([int(v) for v in dims]))
+
+
+def tune_report() -> list[tuple]:
+    """Autotuner decisions: (device, kernel, half-volume, variant, ms)."""
+    buf = C.create_string_buffer(65536)
+    lib.wd_tune_report(buf, len(buf))
+    out = []
+    for line in buf.value.decode().splitlines():
+        d, k, vh, v, ms = line.split()
+        out.append((int(d), k, int(vh), int(v), float(ms)))
+    return out
 
 
 def gen_gauge(dims, seed: int, eps: float = 0.5) -> list[np.ndarray]:
