@@ -1,5 +1,6 @@
 // wd_api.cu -- C ABI: contexts, resident lattices and fields, operators and
 // the host-buffer entry points that replace the reference's functions.
+#include <algorithm>
 #include <cstring>
 #include <cstdio>
 #include <string>
@@ -60,6 +61,8 @@ extern "C" wd_status wd_context_create(int device, wd_context **out)
     ctx->device = device;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->chunk_done[i], cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaMalloc(&ctx->red_partial, sizeof(double2) * (WD_RED_BLOCKS + WD_RED_SLOTS));
     if (e == cudaSuccess) e = cudaHostAlloc(&ctx->red_result, sizeof(double2) * WD_RED_SLOTS, 0);
@@ -137,6 +140,9 @@ extern "C" void wd_context_destroy(wd_context *ctx)
     cudaFree(ctx->red_partial);
     cudaFree(ctx->staging);
     if (ctx->red_result) cudaFreeHost(ctx->red_result);
+    for (auto &ev : ctx->chunk_done)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -523,16 +529,52 @@ static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *
     return WD_OK;
 }
 
+// DslashoffdNew on host arrays, pipelined: only the source parity the
+// hopping term reads (1-cb) is uploaded; the output is computed in chunks of
+// sites, each converted to the reference layout and copied back on the copy
+// stream while the next chunk computes; the other half of dest (zero by the
+// reference's semantics, src/dslash_new.cpp:1398) is cleared on the host in
+// the meantime.
 extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
                                          const double *src, double *dest, int dag, int cb)
 {
     wd_status st = host_prepare(ctx, dims, gauge);
     if (st != WD_OK) return st;
     if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
-    if ((st = wd_field_upload(ctx, ctx->host_f[0], src)) != WD_OK) return st;
-    if ((st = wd_dslash_offd(ctx, ctx->host_lat, ctx->host_f[0], ctx->host_f[1], dag, cb, WD_PREC_F64)) != WD_OK)
-        return st;
-    return wd_field_download(ctx, ctx->host_f[1], dest);
+    if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
+    const wd_lattice *lat = ctx->host_lat;
+    const int Vh = lat->g.Vh;
+    const size_t half = (size_t)12 * Vh;  // complex entries of one parity
+    if ((st = ensure_staging(ctx, 2 * half * sizeof(double2))) != WD_OK) return st;
+    double2 *in_aos = (double2 *)ctx->staging, *out_aos = in_aos + half;
+    double2 *in_blk = ctx->host_f[0]->d + (1 - cb) * half, *out_blk = ctx->host_f[1]->d + cb * half;
+    // upload and convert the source half
+    WD_CUDA(ctx, cudaMemcpyAsync(in_aos, (const double2 *)src + (1 - cb) * half, half * sizeof(double2),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    if ((st = wd_range_aos_to_soa(ctx, ctx->stream, Vh, in_aos, in_blk, 0, Vh)) != WD_OK) return st;
+    // compute and return in chunks
+    const int nchunk = Vh >= 8 * 4096 ? 8 : 1;
+    const int per = (Vh + nchunk - 1) / nchunk;
+    for (int k = 0; k < nchunk; ++k) {
+        const int lo = k * per, hi = std::min(Vh, lo + per);
+        if (lo >= hi) break;
+        if ((st = wd_hop_f64_range(ctx, ctx->stream, lat, in_blk, out_blk, cb, dag, -0.5, lo, hi)) != WD_OK) return st;
+        if ((st = wd_range_soa_to_aos(ctx, ctx->stream, Vh, out_blk, out_aos + (size_t)lo * 12, lo, hi)) != WD_OK)
+            return st;
+        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[k], ctx->stream));
+        WD_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[k], 0));
+        WD_CUDA(ctx, cudaMemcpyAsync((double2 *)dest + cb * half + (size_t)lo * 12, out_aos + (size_t)lo * 12,
+                                     (size_t)(hi - lo) * 12 * sizeof(double2), cudaMemcpyDeviceToHost,
+                                     ctx->copy_stream));
+    }
+    // the untouched parity of dest is zero
+    double *zero = dest + (size_t)(1 - cb) * half * 2;
+    const int64_t nz = (int64_t)half * 2;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < nz; ++i) zero[i] = 0.0;
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return WD_OK;
 }
 
 extern "C" wd_status wd_host_dslash_full(wd_context *ctx, const int dims[4], const double *const gauge[4],

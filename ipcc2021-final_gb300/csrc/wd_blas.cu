@@ -72,6 +72,37 @@ __global__ void __launch_bounds__(256) k_soa_to_aos(const void *__restrict__ soa
     for (int i = threadIdx.x; i < ns * NC; i += blockDim.x) dst[i] = tile[i];
 }
 
+// one parity block, sites [s_lo, s_hi): AoS (12 per site, starting at site s_lo) <-> SoA planes
+__global__ void __launch_bounds__(256) k_range_aos_to_soa(const double2 *__restrict__ aos, double2 *__restrict__ soa,
+                                                          int Vh, int s_lo, int s_hi)
+{
+    __shared__ double2 tile[kTile * 12];
+    const int s0 = s_lo + blockIdx.x * kTile;
+    const int ns = min(kTile, s_hi - s0);
+    const double2 *src = aos + (size_t)(s0 - s_lo) * 12;
+    for (int i = threadIdx.x; i < ns * 12; i += blockDim.x) tile[i] = src[i];
+    __syncthreads();
+    for (int i = threadIdx.x; i < ns * 12; i += blockDim.x) {
+        const int c = i / ns, s = i - c * ns;
+        soa[(size_t)c * Vh + s0 + s] = tile[s * 12 + c];
+    }
+}
+
+__global__ void __launch_bounds__(256) k_range_soa_to_aos(const double2 *__restrict__ soa, double2 *__restrict__ aos,
+                                                          int Vh, int s_lo, int s_hi)
+{
+    __shared__ double2 tile[kTile * 12];
+    const int s0 = s_lo + blockIdx.x * kTile;
+    const int ns = min(kTile, s_hi - s0);
+    for (int i = threadIdx.x; i < ns * 12; i += blockDim.x) {
+        const int c = i / ns, s = i - c * ns;
+        tile[s * 12 + c] = soa[(size_t)c * Vh + s0 + s];
+    }
+    __syncthreads();
+    double2 *dst = aos + (size_t)(s0 - s_lo) * 12;
+    for (int i = threadIdx.x; i < ns * 12; i += blockDim.x) dst[i] = tile[i];
+}
+
 // ------------------------------------------------------- reductions
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -308,6 +339,24 @@ wd_status wd_spinor_soa_to_ref(wd_context *ctx, const WdGeom &g, WdVec soa, doub
 wd_status wd_gauge_ref_to_soa(wd_context *ctx, const WdGeom &g, int mu, const double2 *ref, double2 *soa)
 {
     return to_soa<9>(ctx, g, ref, soa + (size_t)mu * 2 * 9 * g.Vh, WD_PREC_F64);
+}
+
+wd_status wd_range_aos_to_soa(wd_context *ctx, cudaStream_t stream, int Vh, const double2 *aos, double2 *soa_block,
+                              int s_lo, int s_hi)
+{
+    if (s_hi <= s_lo) return WD_OK;
+    k_range_aos_to_soa<<<(s_hi - s_lo + kTile - 1) / kTile, 256, 0, stream>>>(aos, soa_block, Vh, s_lo, s_hi);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}
+
+wd_status wd_range_soa_to_aos(wd_context *ctx, cudaStream_t stream, int Vh, const double2 *soa_block, double2 *aos,
+                              int s_lo, int s_hi)
+{
+    if (s_hi <= s_lo) return WD_OK;
+    k_range_soa_to_aos<<<(s_hi - s_lo + kTile - 1) / kTile, 256, 0, stream>>>(soa_block, aos, Vh, s_lo, s_hi);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
 }
 
 // ---------------------------------------------------------- reductions

@@ -79,3 +79,25 @@ wd_status wd_hop_f64(wd_context *ctx, const wd_lattice *lat, const double2 *in_b
         return run(std::integral_constant<int, 128>());
     });
 }
+
+wd_status wd_hop_f64_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_block,
+                           double2 *out_block, int cb, int dag, double alpha, int s_lo, int s_hi)
+{
+    using P = HopF64<64>;
+    P p;
+    p.g = lat->g;
+    p.cb = cb;
+    p.in = in_block;
+    p.gauge = lat->gauge;
+    p.x = nullptr;
+    p.out = out_block;
+    p.alpha = alpha;
+    p.beta = 0.0;
+    const int n = s_hi - s_lo;
+    if (n <= 0) return WD_OK;
+    const int blocks = (n + P::kThreads - 1) / P::kThreads;
+    if (dag) wd_hop_kernel_range<true><<<blocks, P::kThreads, 0, stream>>>(p, s_lo, s_hi);
+    else wd_hop_kernel_range<false><<<blocks, P::kThreads, 0, stream>>>(p, s_lo, s_hi);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}

@@ -144,3 +144,14 @@ __global__ void __launch_bounds__(P::kThreads) wd_hop_kernel(const P p)
     wd_hop_site<DAG>(p, s, acc);
     p.epilogue(s, acc);
 }
+
+// The same over output sites [s_lo, s_hi) only (pipelined host-buffer path).
+template <bool DAG, class P>
+__global__ void __launch_bounds__(P::kThreads) wd_hop_kernel_range(const P p, int s_lo, int s_hi)
+{
+    const int s = s_lo + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= s_hi) return;
+    typename P::C acc[12];
+    wd_hop_site<DAG>(p, s, acc);
+    p.epilogue(s, acc);
+}

@@ -81,3 +81,19 @@ def test_bad_dims_and_mismatch(wd, ctx):
     with pytest.raises(wd.WilsonError) as e:
         la.dslash_full(la.field(), lb.field(), 0.1, 0)
     assert e.value.status == wd.BAD_ARG
+
+
+@pytest.mark.parametrize("dag,cb", [(0, 0), (1, 1)])
+def test_host_offd_pipelined_large(wd, ctx, oracle, dag, cb):
+    """16^4: the host-buffer DslashoffdNew runs in 8 overlapped chunks; the
+    untouched parity of dest must come back zero whatever it held before."""
+    dims = (16, 16, 16, 16)
+    gauge = wd.gen_gauge(dims, seed=5)
+    src = wd.gen_source(dims, seed=5)
+    out = np.full_like(src, np.nan + 1j)
+    from wilson_gb300 import _dims, _gauge_ptrs, _ptr, lib
+    ctx.check(lib.wd_host_dslash_offd(ctx.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(src), _ptr(out), dag, cb))
+    ref = oracle.dslash_offd(src, gauge, dims, dag, cb)
+    assert rel_l2(out, ref) < TOL
+    half = src.size // 2
+    assert np.all(out[(1 - cb) * half:(2 - cb) * half] == 0)
