@@ -62,7 +62,9 @@ extern "C" wd_status wd_context_create(int device, wd_context **out)
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->h2d_stream, cudaStreamNonBlocking);
     for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->chunk_done[i], cudaEventDisableTiming);
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->chunk_in[i], cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaMalloc(&ctx->red_partial, sizeof(double2) * (WD_RED_BLOCKS + WD_RED_SLOTS));
     if (e == cudaSuccess) e = cudaHostAlloc(&ctx->red_result, sizeof(double2) * WD_RED_SLOTS, 0);
@@ -142,7 +144,10 @@ extern "C" void wd_context_destroy(wd_context *ctx)
     if (ctx->red_result) cudaFreeHost(ctx->red_result);
     for (auto &ev : ctx->chunk_done)
         if (ev) cudaEventDestroy(ev);
+    for (auto &ev : ctx->chunk_in)
+        if (ev) cudaEventDestroy(ev);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -529,12 +534,14 @@ static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *
     return WD_OK;
 }
 
-// DslashoffdNew on host arrays, pipelined: only the source parity the
-// hopping term reads (1-cb) is uploaded; the output is computed in chunks of
-// sites, each converted to the reference layout and copied back on the copy
-// stream while the next chunk computes; the other half of dest (zero by the
-// reference's semantics, src/dslash_new.cpp:1398) is cleared on the host in
-// the meantime.
+// DslashoffdNew on host arrays, as a three-stage pipeline over chunks of
+// time slabs: the upload of source chunk k+1 (h2d stream), the hopping term
+// of output chunk k (compute stream) and the download of output chunk k-1
+// (copy stream) overlap.  Output chunk j reads source chunks j-1..j+1 (the
+// hopping term reaches one slab in t), so it waits for the upload of the
+// latest of those.  Only the source parity the term reads (1-cb) is
+// uploaded, and the other parity of dest -- zero by the reference's
+// semantics, src/dslash_new.cpp:1398 -- is cleared on the host meanwhile.
 extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
                                          const double *src, double *dest, int dag, int cb)
 {
@@ -543,27 +550,40 @@ extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], con
     if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
     if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
     const wd_lattice *lat = ctx->host_lat;
-    const int Vh = lat->g.Vh;
-    const size_t half = (size_t)12 * Vh;  // complex entries of one parity
+    const WdGeom &g = lat->g;
+    const int Vh = g.Vh, Lt = g.L[3];
+    const int slab = g.Lxh * g.L[1] * g.L[2];  // sites of one parity per time slice
+    const size_t half = (size_t)12 * Vh;       // complex entries of one parity
     if ((st = ensure_staging(ctx, 2 * half * sizeof(double2))) != WD_OK) return st;
     double2 *in_aos = (double2 *)ctx->staging, *out_aos = in_aos + half;
     double2 *in_blk = ctx->host_f[0]->d + (1 - cb) * half, *out_blk = ctx->host_f[1]->d + cb * half;
-    // upload and convert the source half
-    WD_CUDA(ctx, cudaMemcpyAsync(in_aos, (const double2 *)src + (1 - cb) * half, half * sizeof(double2),
-                                 cudaMemcpyHostToDevice, ctx->stream));
-    if ((st = wd_range_aos_to_soa(ctx, ctx->stream, Vh, in_aos, in_blk, 0, Vh)) != WD_OK) return st;
-    // compute and return in chunks
-    const int nchunk = Vh >= 8 * 4096 ? 8 : 1;
-    const int per = (Vh + nchunk - 1) / nchunk;
-    for (int k = 0; k < nchunk; ++k) {
-        const int lo = k * per, hi = std::min(Vh, lo + per);
-        if (lo >= hi) break;
+    const double2 *src_half = (const double2 *)src + (1 - cb) * half;
+    double2 *dest_half = (double2 *)dest + cb * half;
+    const int n = (Vh >= 8 * 4096 && Lt >= 3) ? std::min(8, Lt) : 1;
+    int tb[9];
+    for (int k = 0; k <= n; ++k) tb[k] = (int)((int64_t)k * Lt / n);
+    // stage 1: uploads and layout conversion, chunk by chunk
+    for (int k = 0; k < n; ++k) {
+        const int lo = tb[k] * slab, hi = tb[k + 1] * slab;
+        WD_CUDA(ctx, cudaMemcpyAsync(in_aos + (size_t)lo * 12, src_half + (size_t)lo * 12,
+                                     (size_t)(hi - lo) * 12 * sizeof(double2), cudaMemcpyHostToDevice,
+                                     ctx->h2d_stream));
+        if ((st = wd_range_aos_to_soa(ctx, ctx->h2d_stream, Vh, in_aos + (size_t)lo * 12, in_blk, lo, hi)) != WD_OK)
+            return st;
+        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_in[k], ctx->h2d_stream));
+    }
+    // stages 2 and 3: outputs 1..n-2 first, then n-1 and 0 (they need the last upload)
+    for (int i = 0; i < n; ++i) {
+        const int j = n == 1 ? 0 : (i < n - 2 ? i + 1 : (i == n - 2 ? n - 1 : 0));
+        const int need = (n == 1 || j == 0 || j == n - 1) ? n - 1 : j + 1;
+        WD_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->chunk_in[need], 0));
+        const int lo = tb[j] * slab, hi = tb[j + 1] * slab;
         if ((st = wd_hop_f64_range(ctx, ctx->stream, lat, in_blk, out_blk, cb, dag, -0.5, lo, hi)) != WD_OK) return st;
         if ((st = wd_range_soa_to_aos(ctx, ctx->stream, Vh, out_blk, out_aos + (size_t)lo * 12, lo, hi)) != WD_OK)
             return st;
-        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[k], ctx->stream));
-        WD_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[k], 0));
-        WD_CUDA(ctx, cudaMemcpyAsync((double2 *)dest + cb * half + (size_t)lo * 12, out_aos + (size_t)lo * 12,
+        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[j], ctx->stream));
+        WD_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[j], 0));
+        WD_CUDA(ctx, cudaMemcpyAsync(dest_half + (size_t)lo * 12, out_aos + (size_t)lo * 12,
                                      (size_t)(hi - lo) * 12 * sizeof(double2), cudaMemcpyDeviceToHost,
                                      ctx->copy_stream));
     }
@@ -574,6 +594,7 @@ extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], con
     for (int64_t i = 0; i < nz; ++i) zero[i] = 0.0;
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->h2d_stream));
     return WD_OK;
 }
 

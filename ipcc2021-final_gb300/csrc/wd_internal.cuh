@@ -29,7 +29,9 @@ struct wd_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // device->host copies overlapped with compute
+    cudaStream_t h2d_stream = nullptr;   // host->device copies overlapped with compute
     cudaEvent_t chunk_done[8] = {};      // compute -> copy hand-off of the pipelined host path
+    cudaEvent_t chunk_in[8] = {};        // upload -> compute hand-off
     std::string last_error;
     uint64_t launches = 0;
     // scratch: reduction partials (double2 per block) and the staging area
