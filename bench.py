@@ -520,6 +520,13 @@ def run_ours(args) -> None:
             line["solver"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, dims))}, "
                                           f"mass {MASS}, seed 2",
                               **solver_bench(wd, ctx, lat, src, MASS)}
+        if args.solver_dims:
+            sd = tuple(args.solver_dims)
+            slat = ctx.lattice(sd, wd.gen_gauge(sd, SEED, EPS))
+            line["solver_large"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, sd))}, "
+                                                f"mass {args.solver_mass}, seed 2",
+                                    **solver_bench(wd, ctx, slat, wd.gen_source(sd, SEED), args.solver_mass)}
+            slat.close()
         if not args.no_batch:
             line["batch"] = batch_bench(wd, ctx)
         if args.serve_requests > 0:
@@ -543,6 +550,9 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true", help="skip the CG solves/s measurements")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurements")
+    ap.add_argument("--solver-dims", type=int, nargs=4, default=None,
+                    help="also measure the solvers on this lattice (e.g. 48 48 48 96)")
+    ap.add_argument("--solver-mass", type=float, default=0.01)
     ap.add_argument("--serve-requests", type=int, default=24,
                     help="requests per serving run (the configured workload has 2000; 0 skips serving)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[8.0],
