@@ -264,6 +264,14 @@ wd_status wd_host_check(wd_context *ctx, const int dims[4], const double *const 
  * WD_TUNE_CACHE=<file> persists decisions. */
 int wd_tune_report(char *buf, int len);
 void wd_tune_enable(int on);
+/* Pin the launch variant of one kernel ("hop_f64", "hop_df64", "hop_f32",
+ * "hop_f16") for one device and half-volume, bypassing the timing (every
+ * variant computes bit-identical results; only the launch shape differs).
+ * variant < 0 removes the pin.  Returns 0, or -1 for a bad argument or a
+ * variant beyond the kernel's count once that count is known. */
+int wd_tune_pin(int device, const char *kernel, int half_volume, int variant);
+/* Number of launch variants of a kernel, known after its first launch (else 0). */
+int wd_tune_variants(const char *kernel);
 
 /* ---- seeded synthetic inputs (host, deterministic) ---------------------- */
 /* Gauge links U = exp(i eps H) re-unitarised to SU(3), H Gaussian traceless

@@ -85,6 +85,109 @@ __device__ __forceinline__ void split_dir(const SplitDF &p, int s, const WdSite 
     wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
 }
 
+// Software-pipelined form: the loads of the next direction are issued
+// before the arithmetic of the current one, so two directions' memory
+// latency overlap in every warp (more registers, fewer warps).
+struct DirLoad {
+    dfc s[4];  // spin components (k, col) of the neighbour
+    dfc w[3];  // W[col][col], W[col][c1], W[col][c2] as stored (conjugated on use backward)
+};
+
+struct SplitCtx {
+    int s, col, c1, c2, src1, src2;
+    bool on;
+    WdSite cs;
+};
+
+template <int MU, bool FWD>
+__device__ __forceinline__ void split_load(const SplitDF &p, const SplitCtx &x, DirLoad &L)
+{
+    const size_t Vh = p.g.Vh;
+    const int nb = wd_neighbour(p.g, x.s, x.cs, MU, FWD);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) L.s[k] = ld(p.in, (size_t)(k * 3 + x.col) * Vh + nb, x.on);
+    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? x.s : nb);
+    if constexpr (FWD) {
+        L.w[0] = ld(gb, (size_t)(x.col * 3 + x.col) * Vh, x.on);
+        L.w[1] = ld(gb, (size_t)(x.col * 3 + x.c1) * Vh, x.on);
+        L.w[2] = ld(gb, (size_t)(x.col * 3 + x.c2) * Vh, x.on);
+    } else {
+        L.w[0] = ld(gb, (size_t)(x.col * 3 + x.col) * Vh, x.on);
+        L.w[1] = ld(gb, (size_t)(x.c1 * 3 + x.col) * Vh, x.on);
+        L.w[2] = ld(gb, (size_t)(x.c2 * 3 + x.col) * Vh, x.on);
+    }
+}
+
+template <int MU, bool FWD, bool DAG>
+__device__ __forceinline__ void split_compute(const SplitCtx &x, const DirLoad &L, dfc *acc)
+{
+    constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
+    dfc h0, h1;
+    wd_proj1<MU, SG>(L.s[0], L.s[1], L.s[2], L.s[3], h0, h1);
+    const dfc h0b = shfl_dfc(h0, x.src1), h1b = shfl_dfc(h1, x.src1);
+    const dfc h0c = shfl_dfc(h0, x.src2), h1c = shfl_dfc(h1, x.src2);
+    dfc t0, t1;
+    if constexpr (FWD) {
+        t0 = c_madd(c_madd(c_mul(L.w[0], h0), L.w[1], h0b), L.w[2], h0c);
+        t1 = c_madd(c_madd(c_mul(L.w[0], h1), L.w[1], h1b), L.w[2], h1c);
+    } else {
+        t0 = c_maddc(c_maddc(c_mulc(L.w[0], h0), L.w[1], h0b), L.w[2], h0c);
+        t1 = c_maddc(c_maddc(c_mulc(L.w[0], h1), L.w[1], h1b), L.w[2], h1c);
+    }
+    wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
+}
+
+template <bool DAG, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_hop_df_pipe(const SplitDF p)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int cq = lane / kSitesPerWarp;
+    const int ls = lane - cq * kSitesPerWarp;
+    const int s_raw = (blockIdx.x * WARPS + warp) * kSitesPerWarp + ls;
+    SplitCtx x;
+    x.on = cq < 3 && s_raw < p.g.Vh;
+    x.col = cq < 3 ? cq : 0;
+    x.s = x.on ? s_raw : 0;
+    x.c1 = x.col == 2 ? 0 : x.col + 1;
+    x.c2 = x.col == 0 ? 2 : x.col - 1;
+    x.src1 = ls + kSitesPerWarp * x.c1;
+    x.src2 = ls + kSitesPerWarp * x.c2;
+    x.cs = wd_site(p.g, x.s, p.cb);
+    dfc acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfc());
+    DirLoad A, B;
+    split_load<0, true>(p, x, A);
+    split_load<0, false>(p, x, B);
+    split_compute<0, true, DAG>(x, A, acc);
+    split_load<1, true>(p, x, A);
+    split_compute<0, false, DAG>(x, B, acc);
+    split_load<1, false>(p, x, B);
+    split_compute<1, true, DAG>(x, A, acc);
+    split_load<2, true>(p, x, A);
+    split_compute<1, false, DAG>(x, B, acc);
+    split_load<2, false>(p, x, B);
+    split_compute<2, true, DAG>(x, A, acc);
+    split_load<3, true>(p, x, A);
+    split_compute<2, false, DAG>(x, B, acc);
+    split_load<3, false>(p, x, B);
+    split_compute<3, true, DAG>(x, A, acc);
+    split_compute<3, false, DAG>(x, B, acc);
+    if (!x.on) return;
+    const size_t Vh = p.g.Vh;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t i = (size_t)(k * 3 + x.col) * Vh + x.s;
+        dfc r{df_mul(p.alpha, acc[k].re), df_mul(p.alpha, acc[k].im)};
+        if (p.x) {
+            const dfc v = df_from_f4(p.x[i]);
+            r.re = df_madd(r.re, p.beta, v.re);
+            r.im = df_madd(r.im, p.beta, v.im);
+        }
+        p.out[i] = df_to_f4(r);
+    }
+}
+
 template <bool DAG, int WARPS, int MINB>
 __global__ void __launch_bounds__(32 * WARPS, MINB) k_hop_df_split(const SplitDF p)
 {
@@ -167,13 +270,23 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
         WD_LAUNCHED(ctx);
         return WD_OK;
     };
-    using I = std::integral_constant<int, 0>;
-    // variants: 4 warps/block; 2; 8; 4 warps with 6 blocks per SM (80 registers)
-    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 4, [&](int v) -> wd_status {
+    auto run_pipe = [&](auto warps) -> wd_status {
+        constexpr int W = decltype(warps)::value;
+        const int sites_per_block = kSitesPerWarp * W;
+        const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
+        if (dag) k_hop_df_pipe<true, W><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        else k_hop_df_pipe<false, W><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
+    // variants: 4 warps/block; 2; 8; 4 warps with 6 blocks per SM (80 registers);
+    // software-pipelined with 4 and 2 warps per block
+    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 6, [&](int v) -> wd_status {
         if (v == 1) return run(std::integral_constant<int, 2>(), std::integral_constant<int, 1>());
         if (v == 2) return run(std::integral_constant<int, 8>(), std::integral_constant<int, 1>());
         if (v == 3) return run(std::integral_constant<int, 4>(), std::integral_constant<int, 6>());
-        (void)I();
+        if (v == 4) return run_pipe(std::integral_constant<int, 4>());
+        if (v == 5) return run_pipe(std::integral_constant<int, 2>());
         return run(std::integral_constant<int, 4>(), std::integral_constant<int, 1>());
     });
 }

@@ -22,6 +22,7 @@ struct Tuner {
     std::mutex mu;
     std::map<std::tuple<int, std::string, int>, int> best;  // (device, kernel, Vh) -> variant
     std::map<std::tuple<int, std::string, int>, float> best_ms;
+    std::map<std::string, int> variants;  // kernel -> number of launch variants (seen at launch)
     bool loaded = false;
     int enabled = -1;
 
@@ -77,6 +78,7 @@ wd_status wd_tune_launch(wd_context *ctx, const char *kernel, int Vh, int nvaria
     {
         std::lock_guard<std::mutex> lock(T.mu);
         T.load();
+        T.variants[kernel] = nvariants;
         auto it = T.best.find({ctx->device, kernel, Vh});
         if (it != T.best.end()) choice = it->second;
         else if (!T.on() || nvariants <= 1) choice = 0;
@@ -138,6 +140,34 @@ extern "C" int wd_tune_report(char *buf, int len)
         buf[n] = 0;
     }
     return (int)s.size();
+}
+
+extern "C" int wd_tune_pin(int device, const char *kernel, int half_volume, int variant)
+{
+    if (!kernel || half_volume <= 0) return -1;
+    Tuner &T = tuner();
+    std::lock_guard<std::mutex> lock(T.mu);
+    T.load();
+    const auto key = std::make_tuple(device, std::string(kernel), half_volume);
+    if (variant < 0) {
+        T.best.erase(key);
+        T.best_ms.erase(key);
+        return 0;
+    }
+    auto it = T.variants.find(kernel);
+    if (it != T.variants.end() && variant >= it->second) return -1;
+    T.best[key] = variant;
+    T.best_ms[key] = -1.0f;  // pinned, not timed
+    return 0;
+}
+
+extern "C" int wd_tune_variants(const char *kernel)
+{
+    if (!kernel) return 0;
+    Tuner &T = tuner();
+    std::lock_guard<std::mutex> lock(T.mu);
+    auto it = T.variants.find(kernel);
+    return it == T.variants.end() ? 0 : it->second;
 }
 
 extern "C" void wd_tune_enable(int on)

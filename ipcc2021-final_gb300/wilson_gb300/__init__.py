@@ -107,6 +107,8 @@ def _load() -> C.CDLL:
         "wd_server_status": (C.c_int, [vp, ip, ip, dp]),
         "wd_tune_report": (C.c_int, [C.c_char_p, C.c_int]),
         "wd_tune_enable": (None, [C.c_int]),
+        "wd_tune_pin": (C.c_int, [C.c_int, C.c_char_p, C.c_int, C.c_int]),
+        "wd_tune_variants": (C.c_int, [C.c_char_p]),
         "wd_gen_gauge": (C.c_int, [ip, C.c_uint64, C.c_double, d4]),
         "wd_gen_source": (C.c_int, [ip, C.c_uint64, vp]),
     }
@@ -155,6 +157,17 @@ def tune_report() -> list[tuple]:
         d, k, vh, v, ms = line.split()
         out.append((int(d), k, int(vh), int(v), float(ms)))
     return out
+
+
+def tune_pin(kernel: str, half_volume: int, variant: int, device: int = 0) -> None:
+    """Pin a hopping kernel's launch variant for one half-volume (variant < 0 unpins)."""
+    if lib.wd_tune_pin(device, kernel.encode(), half_volume, variant) != 0:
+        raise ValueError(f"cannot pin {kernel} variant {variant} at half-volume {half_volume}")
+
+
+def tune_variants(kernel: str) -> int:
+    """Launch variants of a hopping kernel (0 until it has launched once)."""
+    return lib.wd_tune_variants(kernel.encode())
 
 
 def gen_gauge(dims, seed: int, eps: float = 0.5) -> list[np.ndarray]:
