@@ -183,20 +183,34 @@ def dslash_variants(wd, ctx, lat, src, stream, steps: int, vh: int, peak: float)
     return out
 
 
-def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10) -> dict:
+SOLVER_PLANS = ("f64", "df64", "mixed_f32", "mixed_f16", "mixed_f16_df64")
+
+
+def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10, plans=SOLVER_PLANS,
+                 profile: bool = False) -> dict:
     """One solve per arithmetic on the resident lattice: solves/s, iterations,
-    FP64 true residual, and the relative difference to the FP64 solution."""
+    FP64 true residual, and the relative difference to the FP64 solution.
+    profile=True brackets each timed solve with cudaProfilerStart/Stop (for
+    `ncu --profile-from-start off`)."""
+    import torch
+
     b = lat.field(src)
     out = {}
     ref = None
-    plans = [("f64", wd.F64, wd.F64), ("df64", wd.DF64, wd.F64), ("mixed_f32", wd.F32, wd.F64),
-             ("mixed_f16", wd.F16, wd.F64), ("mixed_f16_df64", wd.F16, wd.DF64)]
-    for name, prec, rel in plans:
+    table = {"f64": (wd.F64, wd.F64), "df64": (wd.DF64, wd.F64), "mixed_f32": (wd.F32, wd.F64),
+             "mixed_f16": (wd.F16, wd.F64), "mixed_f16_df64": (wd.F16, wd.DF64)}
+    for name in plans:
+        prec, rel = table[name]
         x = lat.field()
         p = wd.solver_params(kind=wd.CG_EO, mass=mass, tol=tol, max_iter=5000, prec=prec, prec_reliable=rel)
         lat.solve(b, x, p)            # warm-up (derived link copies, allocator)
         x.zero()
+        ctx.sync()
+        if profile:
+            torch.cuda.profiler.start()
         st = lat.solve(b, x, p)
+        if profile:
+            torch.cuda.profiler.stop()
         sol = x.download()
         if ref is None:
             ref = sol
@@ -204,7 +218,10 @@ def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10) -> dict:
                      "reliable_updates": st.reliable_updates, "true_residual": st.true_residual,
                      "rel_diff_vs_f64": float(np.linalg.norm(sol - ref) / np.linalg.norm(ref))}
         x.close()
-    out["speedup_mixed_f16_vs_f64"] = out["f64"]["seconds"] / out["mixed_f16"]["seconds"]
+    if "f64" in out:
+        for name in out:
+            if name != "f64":
+                out[name]["speedup_vs_f64"] = out["f64"]["seconds"] / out[name]["seconds"]
     return out
 
 
@@ -519,13 +536,15 @@ def run_ours(args) -> None:
         if not args.no_solver:
             line["solver"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, dims))}, "
                                           f"mass {MASS}, seed 2",
-                              **solver_bench(wd, ctx, lat, src, MASS)}
-        if args.solver_dims:
+                              **solver_bench(wd, ctx, lat, src, MASS, plans=args.solver_plans,
+                                             profile=args.profile_solves)}
+        if not args.no_solver_mixed:
             sd = tuple(args.solver_dims)
             slat = ctx.lattice(sd, wd.gen_gauge(sd, SEED, EPS))
-            line["solver_large"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, sd))}, "
+            line["solver_mixed"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, sd))}, "
                                                 f"mass {args.solver_mass}, seed 2",
-                                    **solver_bench(wd, ctx, slat, wd.gen_source(sd, SEED), args.solver_mass)}
+                                    **solver_bench(wd, ctx, slat, wd.gen_source(sd, SEED), args.solver_mass,
+                                                   plans=args.solver_plans, profile=args.profile_solves)}
             slat.close()
         if not args.no_batch:
             line["batch"] = batch_bench(wd, ctx)
@@ -550,9 +569,13 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-solver", action="store_true", help="skip the CG solves/s measurements")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solve measurements")
-    ap.add_argument("--solver-dims", type=int, nargs=4, default=None,
-                    help="also measure the solvers on this lattice (e.g. 48 48 48 96)")
+    ap.add_argument("--solver-plans", nargs="*", choices=SOLVER_PLANS, default=list(SOLVER_PLANS))
+    ap.add_argument("--profile-solves", action="store_true",
+                    help="bracket each timed solve with cudaProfilerStart/Stop (ncu --profile-from-start off)")
+    ap.add_argument("--solver-dims", type=int, nargs=4, default=[32, 32, 32, 64],
+                    help="lattice of the second solver measurement (mixed-precision configuration; 48 48 48 96 also)")
     ap.add_argument("--solver-mass", type=float, default=0.01)
+    ap.add_argument("--no-solver-mixed", action="store_true", help="skip the second solver measurement")
     ap.add_argument("--serve-requests", type=int, default=24,
                     help="requests per serving run (the configured workload has 2000; 0 skips serving)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[8.0],

@@ -64,6 +64,7 @@ struct BTable {
 template <class Sp, class Lk>
 struct BatchHop {
     using C = float2;
+    static constexpr bool kSiteScale = Sp::kScaled;
     WdGeom g;
     int cb;
     Sp in, out, x;
@@ -71,6 +72,12 @@ struct BatchHop {
     bool has_x;
     float alpha, beta;
     __device__ __forceinline__ void load_in(int s, C *v) const { in.load(s, v); }
+    __device__ __forceinline__ float load_in_raw(int s, C *v) const
+    {
+        if constexpr (Sp::kScaled) return in.load_raw(s, v);
+        in.load(s, v);
+        return 1.f;
+    }
     __device__ __forceinline__ void load_link(int mu, int par, int s, C *U) const { link.load(mu, par, s, U); }
 };
 
@@ -118,10 +125,11 @@ __global__ void __launch_bounds__(kSites * kSysPerBlock) k_batch_hop(const BTabl
     float2 r12[12];
     if (S.x) {
         float2 xv[12];
-        if constexpr (F16) SpF16{(uint4 *)S.x, S.x_scale, Vh}.load(s, xv);
+        float bx = be;  // beta times the x site's scale
+        if constexpr (F16) bx *= SpF16{(uint4 *)S.x, S.x_scale, Vh}.load_raw(s, xv);
         else SpF32{(float4 *)S.x, Vh}.load(s, xv);
 #pragma unroll
-        for (int c = 0; c < 12; ++c) r12[c] = c_axpby(al, acc[c], be, xv[c]);
+        for (int c = 0; c < 12; ++c) r12[c] = c_axpby(al, acc[c], bx, xv[c]);
     } else {
 #pragma unroll
         for (int c = 0; c < 12; ++c) r12[c] = c_scale(acc[c], al);
@@ -403,27 +411,14 @@ static inline void slices(EngineSys &s, WdVec &b_e, WdVec &b_o, WdVec &x_e, WdVe
     x_o = wd_offset(s.B.hx.v, (int64_t)12 * Vh, Vh);
 }
 
-// reliable update: x_e += x_s; s = bhat - Mhat x_e; r = Mhat^dag s; r_s <- r (p <- r on a restart)
+// reliable update: x_e += x_s; s = bhat - Mhat x_e; r_s = Mhat^dag s (FP32); p <- r_s on a restart
 wd_status BatchEngine::reliable(EngineSys &s, bool reset_p, double *rr, double *ss)
 {
-    const int Vh = s.lat->g.Vh;
-    const int64_t nh = (int64_t)12 * Vh;
     SysBufs &B = s.B;
     WdVec b_e, b_o, x_e, x_o;
     slices(s, b_e, b_o, x_e, x_o);
-    wd_status e;
-    if ((e = wd_mx_accum(ctx_, Vh, H_, B.xs.v, x_e)) != WD_OK) return e;
-    if ((e = wd_apply_Mhat_v(ctx_, s.lat, x_e, B.t_h.v, B.tmp_oh.v, s.mass, 0)) != WD_OK) return e;
-    if ((e = wd_v_xpayz(ctx_, B.bhat.v, make_double2(-1.0, 0.0), B.t_h.v, B.s_e.v, nh)) != WD_OK) return e;
-    if ((e = wd_apply_Mhat_v(ctx_, s.lat, B.s_e.v, B.r_h.v, B.tmp_oh.v, s.mass, 1)) != WD_OK) return e;
-    if ((e = wd_v_norm2(ctx_, B.r_h.v, nh, 0)) != WD_OK) return e;
-    if ((e = wd_v_norm2(ctx_, B.s_e.v, nh, 1)) != WD_OK) return e;
-    double2 v[2];
-    if ((e = wd_red_fetch(ctx_, 2, v)) != WD_OK) return e;
-    *rr = v[0].x;
-    *ss = v[1].x;
-    // r_s <- r; p <- r on a restart (otherwise t, rewritten next iteration, takes the copy)
-    return wd_mx_from_h(ctx_, Vh, L_, H_, B.r_h.v, B.rs.v, reset_p ? B.p.v : B.t.v);
+    const WdMxReliable rv{B.xs.v, x_e, B.bhat.v, B.t_h.v, B.s_e.v, B.tmp_oh.v, B.r_h.v, B.rs.v};
+    return wd_mx_reliable(ctx_, s.lat, s.mass, L_, H_, rv, reset_p ? &B.p.v : nullptr, rr, ss);
 }
 
 wd_status BatchEngine::add(int tag, const wd_lattice *lat, const double2 *src, double2 *dest, double mass,
@@ -910,6 +905,10 @@ extern "C" wd_status wd_server_add_lattice(wd_server *sv, const int dims[4], con
     if (sv->cfg.prec != WD_PREC_F64) {
         if ((st = wd_lattice_gauge_lp(sv->ctx, lat, sv->cfg.prec)) != WD_OK) return st;
         bytes += (double)lat->volume * 4 * (sv->cfg.prec == WD_PREC_F16 ? 24 : 48);
+        if (sv->cfg.prec == WD_PREC_F16) {  // reliable updates apply Mhat^dag with FP32 links
+            if ((st = wd_lattice_gauge_lp(sv->ctx, lat, WD_PREC_F32)) != WD_OK) return st;
+            bytes += (double)lat->volume * 4 * 48;
+        }
         if (sv->cfg.prec_reliable == WD_PREC_DF64) {
             if ((st = wd_lattice_gauge_df(sv->ctx, lat)) != WD_OK) return st;
             bytes += (double)lat->volume * 4 * 9 * sizeof(float4);

@@ -18,6 +18,7 @@ template <class Sp, class Lk, int THREADS = 128>
 struct HopLP {
     using C = float2;
     static constexpr int kThreads = THREADS;
+    static constexpr bool kSiteScale = Sp::kScaled;
     WdGeom g;
     int cb;
     Sp in, out, x;
@@ -26,15 +27,23 @@ struct HopLP {
     float alpha, beta;
 
     __device__ __forceinline__ void load_in(int s, C *v) const { in.load(s, v); }
+    __device__ __forceinline__ float load_in_raw(int s, C *v) const
+    {
+        if constexpr (Sp::kScaled) return in.load_raw(s, v);
+        in.load(s, v);
+        return 1.f;
+    }
     __device__ __forceinline__ void load_link(int mu, int par, int s, C *U) const { link.load(mu, par, s, U); }
     __device__ __forceinline__ void epilogue(int s, const C *acc) const
     {
         C r[12];
         if (has_x) {
             C xv[12];
-            x.load(s, xv);
+            float bx = beta;  // beta times the x site's scale
+            if constexpr (Sp::kScaled) bx *= x.load_raw(s, xv);
+            else x.load(s, xv);
 #pragma unroll
-            for (int c = 0; c < 12; ++c) r[c] = c_axpby(alpha, acc[c], beta, xv[c]);
+            for (int c = 0; c < 12; ++c) r[c] = c_axpby(alpha, acc[c], bx, xv[c]);
         } else {
 #pragma unroll
             for (int c = 0; c < 12; ++c) r[c] = c_scale(acc[c], alpha);

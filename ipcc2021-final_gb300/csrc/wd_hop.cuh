@@ -11,9 +11,21 @@
 //
 // A policy class P supplies the storage format: the complex arithmetic type
 // P::C, loads of a neighbour spinor and of a link matrix, and the epilogue.
+//
+// A storage with a per-site scale (FP16) may instead expose
+// `static constexpr bool kSiteScale = true` and `float load_in_raw(int, C*)`,
+// returning the unscaled components and the site's scale: the scale then
+// rides on the accumulation (one FMA per real) instead of multiplying the 24
+// loaded reals.
 #pragma once
+#include <type_traits>
 #include "wd_internal.cuh"
 #include "wd_complex.cuh"
+
+template <class P, class = void>
+struct wd_site_scaled : std::false_type {};
+template <class P>
+struct wd_site_scaled<P, std::void_t<decltype(P::kSiteScale)>> : std::bool_constant<P::kSiteScale> {};
 
 template <int SG, class C>
 __device__ __forceinline__ C wd_addsg(const C &a, const C &b)
@@ -63,6 +75,38 @@ __device__ __forceinline__ void wd_recon1(const C &t0, const C &t1, C &d0, C &d1
     }
 }
 
+// d + k t and d + k (i t), k real (FP32 complex only)
+__device__ __forceinline__ float2 wd_cfma(float k, float2 t, float2 d)
+{
+    return make_float2(fmaf(k, t.x, d.x), fmaf(k, t.y, d.y));
+}
+__device__ __forceinline__ float2 wd_cfma_i(float k, float2 t, float2 d)
+{
+    return make_float2(fmaf(-k, t.y, d.x), fmaf(k, t.x, d.y));
+}
+
+// wd_recon1 with the neighbour's scale k folded in: d += k * (the same terms)
+template <int MU, int SG>
+__device__ __forceinline__ void wd_recon1_scaled(float2 t0, float2 t1, float k, float2 &d0, float2 &d1, float2 &d2,
+                                                 float2 &d3)
+{
+    d0 = wd_cfma(k, t0, d0);
+    d1 = wd_cfma(k, t1, d1);
+    if constexpr (MU == 0) {
+        d2 = wd_cfma_i(-SG * k, t1, d2);
+        d3 = wd_cfma_i(-SG * k, t0, d3);
+    } else if constexpr (MU == 1) {
+        d2 = wd_cfma(SG * k, t1, d2);
+        d3 = wd_cfma(-SG * k, t0, d3);
+    } else if constexpr (MU == 2) {
+        d2 = wd_cfma_i(-SG * k, t0, d2);
+        d3 = wd_cfma_i(SG * k, t1, d3);
+    } else {
+        d2 = wd_cfma(SG * k, t0, d2);
+        d3 = wd_cfma(SG * k, t1, d3);
+    }
+}
+
 // Whole-site forms: sp/acc hold 12 components, index spin*3 + colour.
 template <int MU, int SG, class C>
 __device__ __forceinline__ void wd_proj(const C *sp, C *h0, C *h1)
@@ -84,9 +128,12 @@ __device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, t
 {
     using C = typename P::C;
     constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
+    constexpr bool kScaled = wd_site_scaled<P>::value;
     const int nb = wd_neighbour(p.g, s, c, MU, FWD);
     C sp[12];
-    p.load_in(nb, sp);
+    float sc = 1.f;
+    if constexpr (kScaled) sc = p.load_in_raw(nb, sp);
+    else p.load_in(nb, sp);
     C h0[3], h1[3];
     wd_proj<MU, SG>(sp, h0, h1);
     C U[9];
@@ -115,7 +162,12 @@ __device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, t
             }
         }
     }
-    wd_recon<MU, SG>(t0, t1, acc);
+    if constexpr (kScaled) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) wd_recon1_scaled<MU, SG>(t0[a], t1[a], sc, acc[a], acc[3 + a], acc[6 + a], acc[9 + a]);
+    } else {
+        wd_recon<MU, SG>(t0, t1, acc);
+    }
 }
 
 template <bool DAG, class P>

@@ -36,6 +36,7 @@ __device__ __forceinline__ uint4 pack4(const float2 *v)
 
 // ---------------------------------------------------------- spinor sites
 struct SpF32 {
+    static constexpr bool kScaled = false;
     float4 *p;
     int Vh;
     __device__ __forceinline__ void load(int s, float2 *v) const
@@ -56,14 +57,20 @@ struct SpF32 {
 };
 
 struct SpF16 {
+    static constexpr bool kScaled = true;
     uint4 *p;
     float *scale;
     int Vh;
-    __device__ __forceinline__ void load(int s, float2 *v) const
+    // unscaled components; returns the site's scale
+    __device__ __forceinline__ float load_raw(int s, float2 *v) const
     {
-        const float sc = __ldg(scale + s);
 #pragma unroll
         for (int j = 0; j < 3; ++j) unpack4(__ldg(p + (size_t)j * Vh + s), v + 4 * j);
+        return __ldg(scale + s);
+    }
+    __device__ __forceinline__ void load(int s, float2 *v) const
+    {
+        const float sc = load_raw(s, v);
 #pragma unroll
         for (int c = 0; c < 12; ++c) v[c] = make_float2(v[c].x * sc, v[c].y * sc);
     }

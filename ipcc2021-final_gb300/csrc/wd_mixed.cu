@@ -27,12 +27,36 @@ struct HF64 {
     int Vh;
     __device__ double2 load(int c, int s) const { return p[(size_t)c * Vh + s]; }
     __device__ void store(int c, int s, double2 v) const { p[(size_t)c * Vh + s] = v; }
+    __device__ float2 load_f32(int c, int s) const
+    {
+        const double2 d = load(c, s);
+        return make_float2((float)d.x, (float)d.y);
+    }
+    __device__ void add_f32(int c, int s, float2 v) const
+    {
+        double2 d = load(c, s);
+        d.x += (double)v.x;
+        d.y += (double)v.y;
+        store(c, s, d);
+    }
 };
+// double-float: the FP32 views and the accumulation stay on the FP32 pipe
+// (TwoSum, no FP64 conversions)
 struct HDF {
     float4 *p;
     int Vh;
     __device__ double2 load(int c, int s) const { return df_unpack(p[(size_t)c * Vh + s]); }
     __device__ void store(int c, int s, double2 v) const { p[(size_t)c * Vh + s] = df_pack(v); }
+    __device__ float2 load_f32(int c, int s) const
+    {
+        const float4 v = p[(size_t)c * Vh + s];
+        return make_float2(__fadd_rn(v.x, v.y), __fadd_rn(v.z, v.w));
+    }
+    __device__ void add_f32(int c, int s, float2 v) const
+    {
+        const dfc d = df_from_f4(p[(size_t)c * Vh + s]);
+        p[(size_t)c * Vh + s] = df_to_f4(dfc{df_add(d.re, dfr{v.x, 0.f}), df_add(d.im, dfr{v.y, 0.f})});
+    }
 };
 
 __device__ __forceinline__ dfr df_sq_acc(dfr acc, float2 v)
@@ -104,11 +128,33 @@ __global__ void k_mx_from_h(H in, SpF32 a, SpL b, int Vh)
     {
         float2 v[12];
 #pragma unroll
-        for (int c = 0; c < 12; ++c) {
-            const double2 d = in.load(c, s);
-            v[c] = make_float2((float)d.x, (float)d.y);
-        }
+        for (int c = 0; c < 12; ++c) v[c] = in.load_f32(c, s);
         a.store(s, v);
+        b.store(s, v);
+    }
+}
+
+// high precision -> FP32
+template <class H>
+__global__ void k_mx_to_f32(H in, SpF32 a, int Vh)
+{
+    SITE_STRIDE(s, Vh)
+    {
+        float2 v[12];
+#pragma unroll
+        for (int c = 0; c < 12; ++c) v[c] = in.load_f32(c, s);
+        a.store(s, v);
+    }
+}
+
+// FP32 -> kernel storage
+template <class SpL>
+__global__ void k_mx_f32_to(SpF32 a, SpL b, int Vh)
+{
+    SITE_STRIDE(s, Vh)
+    {
+        float2 v[12];
+        a.load(s, v);
         b.store(s, v);
     }
 }
@@ -123,10 +169,7 @@ __global__ void k_mx_accum(SpF32 xs, H x, int Vh)
         xs.load(s, v);
 #pragma unroll
         for (int c = 0; c < 12; ++c) {
-            double2 d = x.load(c, s);
-            d.x += (double)v[c].x;
-            d.y += (double)v[c].y;
-            x.store(c, s, d);
+            x.add_f32(c, s, v[c]);
             v[c] = make_float2(0.f, 0.f);
         }
         xs.store(s, v);
@@ -185,6 +228,30 @@ struct Mixed {
         WD_LAUNCHED(ctx);
         return WD_OK;
     }
+    wd_status to_f32(WdVec h, WdVec a) const
+    {
+        const int g = site_grid(Vh);
+        if (H == WD_PREC_F64) k_mx_to_f32<<<g, WD_RED_THREADS, 0, ctx->stream>>>(HF64{(double2 *)h.p, Vh}, sp_f32(a, Vh), Vh);
+        else k_mx_to_f32<<<g, WD_RED_THREADS, 0, ctx->stream>>>(HDF{(float4 *)h.p, Vh}, sp_f32(a, Vh), Vh);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    }
+    wd_status f32_to(WdVec a, WdVec p) const
+    {
+        if (L == WD_PREC_F32) {
+            WD_CUDA(ctx, cudaMemcpyAsync(p.p, a.p, (size_t)12 * Vh * sizeof(float2), cudaMemcpyDeviceToDevice, ctx->stream));
+            return WD_OK;
+        }
+        k_mx_f32_to<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(a, Vh), sp_f16(p, Vh), Vh);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    }
+    wd_status norm2_f32(WdVec t) const
+    {
+        k_mx_norm2<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(t, Vh), Vh, (double2 *)ctx->red_partial);
+        WD_LAUNCHED(ctx);
+        return wd_red_finish(ctx, 0);
+    }
     wd_status accum(WdVec xs, WdVec xh) const
     {
         const int g = site_grid(Vh);
@@ -207,6 +274,41 @@ wd_status wd_mx_accum(wd_context *ctx, int Vh, wd_precision H, WdVec xs, WdVec x
 wd_status wd_mx_from_h(wd_context *ctx, int Vh, wd_precision L, wd_precision H, WdVec h, WdVec rs, WdVec p)
 {
     return Mixed{ctx, Vh, L, H}.from_h(h, rs, p);
+}
+
+// Reliable update shared by the solo and batched mixed solvers:
+//   x_e += x_s, x_s = 0            (high precision)
+//   s = bhat - Mhat x_e, ss = |s|^2 (high precision: the true residual)
+//   r_s = Mhat^dag s, rr = |r_s|^2  (FP32: s rounded to FP32, FP32 12-real links)
+//   p <- r_s in kernel storage      (on a restart)
+// Only s decides convergence.  r_s seeds the low-precision iteration, which
+// keeps r_s in FP32 anyway, so an FP32 Mhat^dag adds an error of the same
+// order as the rounding of a high-precision r to FP32, relative to the
+// current residual -- and costs a quarter of a double-float application.
+// scratch_h: one high-precision half-lattice buffer, used as two FP32 ones.
+wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
+                         const WdMxReliable &v, const WdVec *p_restart, double *rr, double *ss)
+{
+    const int Vh = lat->g.Vh;
+    const int64_t nh = (int64_t)12 * Vh;
+    const Mixed mx{ctx, Vh, L, H};
+    WdVec s32, tmp32;
+    s32.prec = tmp32.prec = WD_PREC_F32;
+    s32.p = v.scratch_h.p;
+    tmp32.p = (char *)v.scratch_h.p + (size_t)nh * sizeof(float2);
+    wd_status e;
+    if ((e = mx.accum(v.xs, v.x_e)) != WD_OK) return e;
+    if ((e = wd_apply_Mhat_v(ctx, lat, v.x_e, v.t_h, v.tmp_oh, mass, 0)) != WD_OK) return e;
+    if ((e = wd_v_xpayz(ctx, v.bhat, make_double2(-1.0, 0.0), v.t_h, v.s_e, nh)) != WD_OK) return e;
+    if ((e = mx.to_f32(v.s_e, s32)) != WD_OK) return e;
+    if ((e = wd_apply_Mhat_v(ctx, lat, s32, v.rs, tmp32, mass, 1)) != WD_OK) return e;
+    if ((e = mx.norm2_f32(v.rs)) != WD_OK) return e;
+    if ((e = wd_v_norm2(ctx, v.s_e, nh, 1)) != WD_OK) return e;
+    double2 red[2];
+    if ((e = wd_red_fetch(ctx, 2, red)) != WD_OK) return e;
+    *rr = red[0].x;
+    *ss = red[1].x;
+    return p_restart ? mx.f32_to(v.rs, *p_restart) : WD_OK;
 }
 
 wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const double2 *src, double2 *x,
@@ -236,7 +338,8 @@ wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const dou
         if ((st = wd_vec_alloc(ctx, hs, H, n)) != WD_OK) return st;
         if ((st = wd_vec_alloc(ctx, hx, H, n)) != WD_OK) return st;
         if ((st = wd_convert_f64_to_df(ctx, src, (float4 *)hs.v.p, n)) != WD_OK) return st;
-        if ((st = wd_convert_f64_to_df(ctx, x, (float4 *)hx.v.p, n)) != WD_OK) return st;
+        // without an initial guess x_e is zeroed below and x_o is written at the end
+        if (prm->use_initial_guess && (st = wd_convert_f64_to_df(ctx, x, (float4 *)hx.v.p, n)) != WD_OK) return st;
         vsrc = hs.v;
         vx = hx.v;
     }
@@ -251,22 +354,11 @@ wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const dou
     if ((st = wd_red_fetch(ctx, 2, red)) != WD_OK) return st;
     const double norm_b = red[1].x > 0 ? std::sqrt(red[1].x) : 1.0;
 
-    // reliable update: x_e += x_s; s = bhat - Mhat x_e; r = Mhat^dag s; r_s, p <- r (p only on restart)
+    // reliable update: x_e += x_s; s = bhat - Mhat x_e; r_s = Mhat^dag s (p <- r_s only on a restart)
     double rr = 0, ss = 0;
+    const WdMxReliable rv{xs.v, x_e, bhat.v, t_h.v, s_e.v, tmp_oh.v, r_h.v, rs.v};
     auto reliable = [&](bool reset_p) -> wd_status {
-        wd_status e = mx.accum(xs.v, x_e);
-        if (e != WD_OK) return e;
-        if ((e = wd_apply_Mhat_v(ctx, lat, x_e, t_h.v, tmp_oh.v, m, 0)) != WD_OK) return e;
-        if ((e = wd_v_xpayz(ctx, bhat.v, make_double2(-1.0, 0.0), t_h.v, s_e.v, nh)) != WD_OK) return e;
-        if ((e = wd_apply_Mhat_v(ctx, lat, s_e.v, r_h.v, tmp_oh.v, m, 1)) != WD_OK) return e;
-        if ((e = wd_v_norm2(ctx, r_h.v, nh, 0)) != WD_OK) return e;
-        if ((e = wd_v_norm2(ctx, s_e.v, nh, 1)) != WD_OK) return e;
-        double2 v[2];
-        if ((e = wd_red_fetch(ctx, 2, v)) != WD_OK) return e;
-        rr = v[0].x;
-        ss = v[1].x;
-        // r_s <- r (and p <- r on a restart); otherwise p is kept
-        return mx.from_h(r_h.v, rs.v, reset_p ? p.v : t.v);
+        return wd_mx_reliable(ctx, lat, m, prm->prec, H, rv, reset_p ? &p.v : nullptr, &rr, &ss);
     };
 
     if ((st = reliable(true)) != WD_OK) return st;

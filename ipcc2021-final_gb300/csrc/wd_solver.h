@@ -30,3 +30,17 @@ wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const dou
 wd_status wd_mx_accum(wd_context *ctx, int Vh, wd_precision H, WdVec xs, WdVec xh);
 // rs (FP32) <- h and p (storage L) <- h
 wd_status wd_mx_from_h(wd_context *ctx, int Vh, wd_precision L, wd_precision H, WdVec h, WdVec rs, WdVec p);
+// one system's buffers for a reliable update (even-parity half-lattice blocks)
+struct WdMxReliable {
+    WdVec xs;         // FP32 solution increment (zeroed)
+    WdVec x_e;        // high-precision solution
+    WdVec bhat;       // high-precision Schur source
+    WdVec t_h, s_e;   // high-precision work; s_e receives the true residual
+    WdVec tmp_oh;     // high-precision odd-parity work
+    WdVec scratch_h;  // high-precision work, used as two FP32 blocks
+    WdVec rs;         // FP32 iterated residual, receives Mhat^dag s
+};
+// x_e += xs; s = bhat - Mhat x_e (high); rs = Mhat^dag s (FP32); rr = |rs|^2,
+// ss = |s|^2; p_restart (storage L) <- rs when given
+wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
+                         const WdMxReliable &v, const WdVec *p_restart, double *rr, double *ss);
