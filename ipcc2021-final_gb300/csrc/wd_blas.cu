@@ -264,6 +264,39 @@ __global__ void __launch_bounds__(WD_RED_THREADS) k_cg_update(double2 alpha, con
     block_partial(s, 0.0, partial);
 }
 
+// Real-scalar forms for the even-odd CG, whose alpha and beta are real
+// (ratios of norms): one FMA per real instead of a complex product.
+// y = x + b y
+__global__ void k_xpby_real(const double2 *__restrict__ x, double b, double2 *__restrict__ y, int64_t n)
+{
+    GRID_STRIDE(i, n)
+    {
+        const double2 u = x[i], v = y[i];
+        y[i] = make_double2(fma(b, v.x, u.x), fma(b, v.y, u.y));
+    }
+}
+
+// x += alpha p; r -= alpha q; partial |r|^2
+__global__ void __launch_bounds__(WD_RED_THREADS) k_cg_update_real(double alpha, const double2 *__restrict__ p,
+                                                                   const double2 *__restrict__ q,
+                                                                   double2 *__restrict__ x, double2 *__restrict__ r,
+                                                                   int64_t n, double2 *partial)
+{
+    double s = 0.0;
+    GRID_STRIDE(i, n)
+    {
+        const double2 pv = p[i], qv = q[i];
+        double2 xv = x[i], rv = r[i];
+        xv = make_double2(fma(alpha, pv.x, xv.x), fma(alpha, pv.y, xv.y));
+        rv = make_double2(fma(-alpha, qv.x, rv.x), fma(-alpha, qv.y, rv.y));
+        x[i] = xv;
+        r[i] = rv;
+        s = fma(rv.x, rv.x, s);
+        s = fma(rv.y, rv.y, s);
+    }
+    block_partial(s, 0.0, partial);
+}
+
 // ----------------------------------------------------- double-float BLAS
 __host__ __device__ __forceinline__ dfc dfc_split(double2 a) { return dfc{df_split(a.x), df_split(a.y)}; }
 
@@ -275,6 +308,35 @@ __global__ void k_axpby_df(dfc a, const float4 *__restrict__ x, dfc b, float4 *_
 __global__ void k_xpayz_df(const float4 *__restrict__ x, dfc a, const float4 *y, float4 *z, int64_t n)
 {
     GRID_STRIDE(i, n) { z[i] = df_to_f4(c_madd(df_from_f4(x[i]), a, df_from_f4(y[i]))); }
+}
+
+__global__ void k_xpby_real_df(const float4 *__restrict__ x, dfr b, float4 *__restrict__ y, int64_t n)
+{
+    GRID_STRIDE(i, n)
+    {
+        const dfc u = df_from_f4(x[i]), v = df_from_f4(y[i]);
+        y[i] = df_to_f4(dfc{df_madd(u.re, b, v.re), df_madd(u.im, b, v.im)});
+    }
+}
+
+__global__ void __launch_bounds__(WD_RED_THREADS) k_cg_update_real_df(dfr alpha, dfr malpha,
+                                                                      const float4 *__restrict__ p,
+                                                                      const float4 *__restrict__ q,
+                                                                      float4 *__restrict__ x, float4 *__restrict__ r,
+                                                                      int64_t n, double2 *partial)
+{
+    dfr s{0.f, 0.f};
+    GRID_STRIDE(i, n)
+    {
+        const dfc pv = df_from_f4(p[i]), qv = df_from_f4(q[i]);
+        dfc xv = df_from_f4(x[i]), rv = df_from_f4(r[i]);
+        xv = dfc{df_madd(xv.re, alpha, pv.re), df_madd(xv.im, alpha, pv.im)};
+        rv = dfc{df_madd(rv.re, malpha, qv.re), df_madd(rv.im, malpha, qv.im)};
+        x[i] = df_to_f4(xv);
+        r[i] = df_to_f4(rv);
+        s = df_madd(df_madd(s, rv.re, rv.re), rv.im, rv.im);
+    }
+    block_partial(df_value(s), 0.0, partial);
 }
 
 __global__ void __launch_bounds__(WD_RED_THREADS) k_cg_update_df(dfc alpha, dfc malpha, const float4 *__restrict__ p,
@@ -485,6 +547,34 @@ wd_status wd_v_cg_update(wd_context *ctx, double2 alpha, WdVec p, WdVec q, WdVec
     k_cg_update_df<<<WD_RED_BLOCKS, WD_RED_THREADS, 0, ctx->stream>>>(
         dfc_split(alpha), dfc_split(make_double2(-alpha.x, -alpha.y)), (const float4 *)p.p, (const float4 *)q.p,
         (float4 *)x.p, (float4 *)r.p, n, (double2 *)ctx->red_partial);
+    WD_LAUNCHED(ctx);
+    return wd_red_finish(ctx, slot);
+}
+
+wd_status wd_v_xpby(wd_context *ctx, WdVec x, double b, WdVec y, int64_t n)
+{
+    wd_status st = same_prec(ctx, {x, y});
+    if (st != WD_OK) return st;
+    if (x.prec == WD_PREC_F64)
+        k_xpby_real<<<blas_blocks(n), 256, 0, ctx->stream>>>((const double2 *)x.p, b, (double2 *)y.p, n);
+    else
+        k_xpby_real_df<<<blas_blocks(n), 256, 0, ctx->stream>>>((const float4 *)x.p, df_split(b), (float4 *)y.p, n);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}
+
+wd_status wd_v_cg_update_real(wd_context *ctx, double alpha, WdVec p, WdVec q, WdVec x, WdVec r, int64_t n, int slot)
+{
+    wd_status st = same_prec(ctx, {p, q, x, r});
+    if (st != WD_OK) return st;
+    double2 *part = (double2 *)ctx->red_partial;
+    if (p.prec == WD_PREC_F64)
+        k_cg_update_real<<<WD_RED_BLOCKS, WD_RED_THREADS, 0, ctx->stream>>>(
+            alpha, (const double2 *)p.p, (const double2 *)q.p, (double2 *)x.p, (double2 *)r.p, n, part);
+    else
+        k_cg_update_real_df<<<WD_RED_BLOCKS, WD_RED_THREADS, 0, ctx->stream>>>(
+            df_split(alpha), df_split(-alpha), (const float4 *)p.p, (const float4 *)q.p, (float4 *)x.p,
+            (float4 *)r.p, n, part);
     WD_LAUNCHED(ctx);
     return wd_red_finish(ctx, slot);
 }

@@ -56,6 +56,9 @@ wd_status wd_v_dot(wd_context *ctx, WdVec a, WdVec b, int64_t n, int slot);
 wd_status wd_v_axpby(wd_context *ctx, double2 a, WdVec x, double2 b, WdVec y, int64_t n);
 wd_status wd_v_xpayz(wd_context *ctx, WdVec x, double2 a, WdVec y, WdVec z, int64_t n);
 wd_status wd_v_cg_update(wd_context *ctx, double2 alpha, WdVec p, WdVec q, WdVec x, WdVec r, int64_t n, int slot);
+// real-scalar forms (even-odd CG): y = x + b y; x += alpha p, r -= alpha q, |r|^2 -> slot
+wd_status wd_v_xpby(wd_context *ctx, WdVec x, double b, WdVec y, int64_t n);
+wd_status wd_v_cg_update_real(wd_context *ctx, double alpha, WdVec p, WdVec q, WdVec x, WdVec r, int64_t n, int slot);
 wd_status wd_v_copy(wd_context *ctx, WdVec dst, WdVec src, int64_t n);
 wd_status wd_v_zero(wd_context *ctx, WdVec v, int64_t n);
 

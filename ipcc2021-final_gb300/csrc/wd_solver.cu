@@ -207,7 +207,7 @@ static wd_status cg_eo_core(wd_context *ctx, const wd_lattice *lat, WdVec src, W
         if ((st = wd_v_norm2(ctx, t, nh, 0)) != WD_OK) return st;
         if ((st = fetch1(ctx, red)) != WD_OK) return st;
         const double alpha = rr / red[0].x;
-        if ((st = wd_v_cg_update(ctx, make_double2(alpha, 0.0), p, q, x_e, r, nh, 0)) != WD_OK) return st;
+        if ((st = wd_v_cg_update_real(ctx, alpha, p, q, x_e, r, nh, 0)) != WD_OK) return st;
         if ((st = fetch1(ctx, red)) != WD_OK) return st;
         double rr_new = red[0].x;
         ++iters;
@@ -230,7 +230,7 @@ static wd_status cg_eo_core(wd_context *ctx, const wd_lattice *lat, WdVec src, W
         }
         const double beta = rr_new / rr;
         rr = rr_new;
-        if ((st = wd_v_axpby(ctx, make_double2(1.0, 0.0), r, make_double2(beta, 0.0), p, nh)) != WD_OK) return st;
+        if ((st = wd_v_xpby(ctx, r, beta, p, nh)) != WD_OK) return st;
     }
     // x_o = (b_o + D_oe x_e / 2) / a
     if ((st = wd_hop_v(ctx, lat, x_e, x_o, &b_o, 1, 0, 0.5 / a, 1.0 / a)) != WD_OK) return st;
