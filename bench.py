@@ -366,12 +366,16 @@ def serve_run(wd, ctx, reqs, rate: float, prec: int, budget: float = 150e9, seed
             "max_residual_over_tol": worst}
 
 
-def serve_bench(wd, ctx, n: int, rates_mixed, rates_f64) -> dict:
+def serve_bench(wd, ctx, n: int, rates_mixed, rates_f64, n_f64: int | None = None) -> dict:
+    """The same request stream (its first n_f64 requests for the FP64 server)
+    at each arrival rate."""
     reqs = serve_workload(n)
-    out = {"workload": f"{n} Poisson-arrival requests, sizes {{8^3x16:.4, 16^3x32:.3, 24^3x48:.2, 32^3x64:.1}}, "
-                       "mass U[0.02,0.2], tol {1e-8,1e-10}, 1-12 sources, 8 resident gauge fields, 150 GB budget",
+    reqs64 = reqs[:n_f64] if n_f64 else reqs
+    out = {"workload": f"{n} Poisson-arrival requests ({len(reqs64)} for plain FP64), sizes "
+                       "{8^3x16:.4, 16^3x32:.3, 24^3x48:.2, 32^3x64:.1}, mass U[0.02,0.2], tol {1e-8,1e-10}, "
+                       "1-12 sources, 8 resident gauge fields, 150 GB budget",
            "mixed_batched_f32": [serve_run(wd, ctx, reqs, r, wd.F32) for r in rates_mixed],
-           "plain_f64": [serve_run(wd, ctx, reqs, r, wd.F64) for r in rates_f64]}
+           "plain_f64": [serve_run(wd, ctx, reqs64, r, wd.F64) for r in rates_f64]}
     return out
 
 
@@ -549,7 +553,8 @@ def run_ours(args) -> None:
         if not args.no_batch:
             line["batch"] = batch_bench(wd, ctx)
         if args.serve_requests > 0:
-            line["serving"] = serve_bench(wd, ctx, args.serve_requests, args.serve_rates, args.serve_rates_f64)
+            line["serving"] = serve_bench(wd, ctx, args.serve_requests, args.serve_rates, args.serve_rates_f64,
+                                          args.serve_requests_f64)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_port(gauge, src, dims)
         print(json.dumps(line), flush=True)
@@ -578,6 +583,8 @@ def main() -> None:
     ap.add_argument("--no-solver-mixed", action="store_true", help="skip the second solver measurement")
     ap.add_argument("--serve-requests", type=int, default=24,
                     help="requests per serving run (the configured workload has 2000; 0 skips serving)")
+    ap.add_argument("--serve-requests-f64", type=int, default=None,
+                    help="requests for the plain FP64 server (default: the same stream)")
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[8.0],
                     help="arrival rates (requests/s) for the batched mixed-precision server")
     ap.add_argument("--serve-rates-f64", type=float, nargs="*", default=[3.0],
