@@ -499,9 +499,11 @@ def run_ours(args) -> None:
         e2e = {"value": replica_throughput(BYTES_PER_SITE_F64 * vh, e2e_s, world) / 1e9, "unit": "GB/s",
                "h2d_bytes_per_step": int(src.nbytes // 2), "d2h_bytes_per_step": int(src.nbytes // 2),
                "steps": n_e2e, "ms_per_step": e2e_s * 1e3,
-               "path": "wd_host_dslash_offd (DslashoffdNew): the source parity it reads goes up, the computed "
-                       "parity comes back in 8 chunks overlapped with compute, the other parity of dest is "
-                       "zeroed on the host meanwhile; pinned host buffers, links resident"}
+               "path": "wd_host_dslash_offd (DslashoffdNew): the source parity it reads goes up and the "
+                       "computed parity comes back in up to 16 time-slab chunks overlapped with compute on "
+                       "two streams, the kernel working on the reference's site-major layout in the staging "
+                       "buffers; the other parity of dest is zeroed on the host meanwhile; pinned host "
+                       "buffers, links resident"}
 
     if rank == 0:
         peak, peak_src = measured_peak_hbm()

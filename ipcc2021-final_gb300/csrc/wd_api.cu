@@ -63,8 +63,11 @@ extern "C" wd_status wd_context_create(int device, wd_context **out)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->h2d_stream, cudaStreamNonBlocking);
-    for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->chunk_done[i], cudaEventDisableTiming);
-    for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&ctx->chunk_in[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < WD_MAX_CHUNKS && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&ctx->chunk_done[i], cudaEventDisableTiming);
+    for (int i = 0; i < WD_MAX_UPLOADS && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&ctx->chunk_in[i], cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaMalloc(&ctx->red_partial, sizeof(double2) * (WD_RED_BLOCKS + WD_RED_SLOTS));
     if (e == cudaSuccess) e = cudaHostAlloc(&ctx->red_result, sizeof(double2) * WD_RED_SLOTS, 0);
@@ -148,6 +151,7 @@ extern "C" void wd_context_destroy(wd_context *ctx)
         if (ev) cudaEventDestroy(ev);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->h2d_stream) cudaStreamDestroy(ctx->h2d_stream);
+    if (ctx->aux_stream) cudaStreamDestroy(ctx->aux_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -534,14 +538,19 @@ static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *
     return WD_OK;
 }
 
-// DslashoffdNew on host arrays, as a three-stage pipeline over chunks of
-// time slabs: the upload of source chunk k+1 (h2d stream), the hopping term
-// of output chunk k (compute stream) and the download of output chunk k-1
-// (copy stream) overlap.  Output chunk j reads source chunks j-1..j+1 (the
-// hopping term reaches one slab in t), so it waits for the upload of the
-// latest of those.  Only the source parity the term reads (1-cb) is
-// uploaded, and the other parity of dest -- zero by the reference's
-// semantics, src/dslash_new.cpp:1398 -- is cleared on the host meanwhile.
+// DslashoffdNew on host arrays, as a three-stage pipeline over time slabs:
+// uploads of the source (h2d stream), the hopping term of output chunks (two
+// compute streams) and downloads of finished output chunks (copy stream)
+// overlap.  Output chunk [t0, t1) reads source slices t0-1 .. t1 (the
+// hopping term reaches one slice in t), so it waits only for the upload
+// holding slice t1; uploads go in units of at most Lt/32 slices, enqueued
+// just ahead of the first chunk that needs them, so the first compute starts
+// after about a chunk and a unit have arrived.  Chunk 0 reads slice Lt-1 and
+// runs last.  Only the source parity the term reads (1-cb) is uploaded, and
+// the other parity of dest -- zero by the reference's semantics,
+// src/dslash_new.cpp:1398 -- is cleared on the host meanwhile.  The kernel
+// reads and writes the reference's site-major layout in the staging buffers,
+// so data goes from copy to arithmetic to copy with no layout conversion.
 extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
                                          const double *src, double *dest, int dag, int cb)
 {
@@ -556,44 +565,57 @@ extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], con
     const size_t half = (size_t)12 * Vh;       // complex entries of one parity
     if ((st = ensure_staging(ctx, 2 * half * sizeof(double2))) != WD_OK) return st;
     double2 *in_aos = (double2 *)ctx->staging, *out_aos = in_aos + half;
-    double2 *in_blk = ctx->host_f[0]->d + (1 - cb) * half, *out_blk = ctx->host_f[1]->d + cb * half;
     const double2 *src_half = (const double2 *)src + (1 - cb) * half;
     double2 *dest_half = (double2 *)dest + cb * half;
-    const int n = (Vh >= 8 * 4096 && Lt >= 3) ? std::min(8, Lt) : 1;
-    int tb[9];
+    // compute chunks of at least 64k sites (at most WD_MAX_CHUNKS); upload units
+    int n = std::min(std::min(WD_MAX_CHUNKS, Lt), Vh / 65536);
+    if (n < 3) n = 1;
+    int tb[WD_MAX_CHUNKS + 1];
     for (int k = 0; k <= n; ++k) tb[k] = (int)((int64_t)k * Lt / n);
-    // stage 1: uploads and layout conversion, chunk by chunk
-    for (int k = 0; k < n; ++k) {
-        const int lo = tb[k] * slab, hi = tb[k + 1] * slab;
-        WD_CUDA(ctx, cudaMemcpyAsync(in_aos + (size_t)lo * 12, src_half + (size_t)lo * 12,
-                                     (size_t)(hi - lo) * 12 * sizeof(double2), cudaMemcpyHostToDevice,
-                                     ctx->h2d_stream));
-        if ((st = wd_range_aos_to_soa(ctx, ctx->h2d_stream, Vh, in_aos + (size_t)lo * 12, in_blk, lo, hi)) != WD_OK)
-            return st;
-        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_in[k], ctx->h2d_stream));
-    }
-    // stages 2 and 3: outputs 1..n-2 first, then n-1 and 0 (they need the last upload)
+    const int us = n == 1 ? Lt : (Lt + WD_MAX_UPLOADS - 1) / WD_MAX_UPLOADS;  // slices per upload unit
+    const int nu = (Lt + us - 1) / us;  // upload units (<= WD_MAX_UPLOADS), unit u = slices [u*us, (u+1)*us)
+    int uploaded = 0;                   // units enqueued so far
+    auto upload_through = [&](int unit) -> wd_status {
+        for (; uploaded <= unit; ++uploaded) {
+            const size_t lo = (size_t)uploaded * us * slab * 12;
+            const size_t hi = (size_t)std::min((uploaded + 1) * us, Lt) * slab * 12;
+            WD_CUDA(ctx, cudaMemcpyAsync(in_aos + lo, src_half + lo, (hi - lo) * sizeof(double2),
+                                         cudaMemcpyHostToDevice, ctx->h2d_stream));
+            WD_CUDA(ctx, cudaEventRecord(ctx->chunk_in[uploaded], ctx->h2d_stream));
+        }
+        return WD_OK;
+    };
+    // uploads start after the work already queued on the context's stream
+    WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[0], ctx->stream));
+    WD_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d_stream, ctx->chunk_done[0], 0));
+    // chunks 1..n-1, then 0; consecutive chunks alternate between two compute
+    // streams, so one chunk's last partial wave of blocks overlaps the next's first
     for (int i = 0; i < n; ++i) {
-        const int j = n == 1 ? 0 : (i < n - 2 ? i + 1 : (i == n - 2 ? n - 1 : 0));
-        const int need = (n == 1 || j == 0 || j == n - 1) ? n - 1 : j + 1;
-        WD_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->chunk_in[need], 0));
+        const int j = n == 1 ? 0 : (i + 1) % n;
+        const int need = (j == 0 || tb[j + 1] >= Lt) ? nu - 1 : tb[j + 1] / us;
+        if ((st = upload_through(need)) != WD_OK) return st;
+        cudaStream_t cs = (i & 1) ? ctx->aux_stream : ctx->stream;
+        WD_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->chunk_in[need], 0));
         const int lo = tb[j] * slab, hi = tb[j + 1] * slab;
-        if ((st = wd_hop_f64_range(ctx, ctx->stream, lat, in_blk, out_blk, cb, dag, -0.5, lo, hi)) != WD_OK) return st;
-        if ((st = wd_range_soa_to_aos(ctx, ctx->stream, Vh, out_blk, out_aos + (size_t)lo * 12, lo, hi)) != WD_OK)
-            return st;
-        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[j], ctx->stream));
+        if ((st = wd_hop_f64_aos_range(ctx, cs, lat, in_aos, out_aos, cb, dag, -0.5, lo, hi)) != WD_OK) return st;
+        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[j], cs));
         WD_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[j], 0));
         WD_CUDA(ctx, cudaMemcpyAsync(dest_half + (size_t)lo * 12, out_aos + (size_t)lo * 12,
                                      (size_t)(hi - lo) * 12 * sizeof(double2), cudaMemcpyDeviceToHost,
                                      ctx->copy_stream));
     }
-    // the untouched parity of dest is zero
+    // the untouched parity of dest is zero.  Four threads: the copies to and
+    // from host memory run meanwhile, and a wider team both competes with them
+    // for host memory bandwidth and, on a busy host, waits on descheduled
+    // threads (measured at 32^3x64: 2.03 ms per call with 2-8 threads, up to
+    // 4.4 ms with 16 on 16 cores).
     double *zero = dest + (size_t)(1 - cb) * half * 2;
     const int64_t nz = (int64_t)half * 2;
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(4)
     for (int64_t i = 0; i < nz; ++i) zero[i] = 0.0;
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->aux_stream));
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->h2d_stream));
     return WD_OK;
 }

@@ -49,7 +49,52 @@ struct HopF64 {
     }
 };
 
+// The same kernel on the reference's own site-major layout (AoS: the 12
+// complex components of a site contiguous, [site][spin*3+colour]) for the
+// input and output parity blocks; the links stay in the SoA planes.  A warp's
+// 32 neighbour sites are 6 KB of consecutive bytes, so every fetched line is
+// used, and the FP64 pipe (not the access pattern) still bounds the kernel.
+// The host-buffer path runs it on the staging buffers directly, with no
+// layout conversion between the copies and the arithmetic.
+template <int THREADS>
+struct HopF64AoS : HopF64<THREADS> {
+    __device__ __forceinline__ void load_in(int s, double2 *v) const
+    {
+        const double2 *b = this->in + (size_t)s * 12;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) v[c] = b[c];
+    }
+    __device__ __forceinline__ void epilogue(int s, const double2 *acc) const
+    {
+        double2 *o = this->out + (size_t)s * 12;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) o[c] = c_scale(acc[c], this->alpha);
+    }
+};
+
 }  // namespace
+
+wd_status wd_hop_f64_aos_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_aos,
+                               double2 *out_aos, int cb, int dag, double alpha, int s_lo, int s_hi)
+{
+    using P = HopF64AoS<64>;
+    P p;
+    p.g = lat->g;
+    p.cb = cb;
+    p.in = in_aos;
+    p.gauge = lat->gauge;
+    p.x = nullptr;
+    p.out = out_aos;
+    p.alpha = alpha;
+    p.beta = 0.0;
+    const int n = s_hi - s_lo;
+    if (n <= 0) return WD_OK;
+    const int blocks = (n + P::kThreads - 1) / P::kThreads;
+    if (dag) wd_hop_kernel_range<true><<<blocks, P::kThreads, 0, stream>>>(p, s_lo, s_hi);
+    else wd_hop_kernel_range<false><<<blocks, P::kThreads, 0, stream>>>(p, s_lo, s_hi);
+    WD_LAUNCHED(ctx);
+    return WD_OK;
+}
 
 wd_status wd_hop_f64(wd_context *ctx, const wd_lattice *lat, const double2 *in_block,
                      double2 *out_block, const double2 *x_block, int cb, int dag, double alpha,

@@ -19,6 +19,10 @@
 
 #define WD_MAX_SITES (int64_t(1) << 30)
 
+// compute chunks and upload units of the pipelined host-buffer hopping term
+constexpr int WD_MAX_CHUNKS = 16;
+constexpr int WD_MAX_UPLOADS = 32;
+
 struct WdGeom {
     int L[4];  // Lx, Ly, Lz, Lt
     int Lxh;   // Lx / 2
@@ -30,8 +34,9 @@ struct wd_context {
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;  // device->host copies overlapped with compute
     cudaStream_t h2d_stream = nullptr;   // host->device copies overlapped with compute
-    cudaEvent_t chunk_done[8] = {};      // compute -> copy hand-off of the pipelined host path
-    cudaEvent_t chunk_in[8] = {};        // upload -> compute hand-off
+    cudaStream_t aux_stream = nullptr;   // second compute stream of the pipelined host path
+    cudaEvent_t chunk_done[WD_MAX_CHUNKS] = {};  // compute -> copy hand-off of the pipelined host path
+    cudaEvent_t chunk_in[WD_MAX_UPLOADS] = {};   // upload -> compute hand-off
     std::string last_error;
     uint64_t launches = 0;
     // scratch: reduction partials (double2 per block) and the staging area
