@@ -105,12 +105,14 @@ __device__ __forceinline__ dfr df_norm(dfr a)
 }
 
 // ------------------------------------------------------------- storage
-// A complex df value is stored (normalised) as float4 {re.h, re.l, im.h, im.l}.
-__device__ __forceinline__ dfc df_from_f4(float4 v) { return dfc{{v.x, v.y}, {v.z, v.w}}; }
+// A complex df value is stored (normalised) as float4 {re.h, im.h, re.l, im.l}:
+// the high parts and the low parts each form an adjacent (re, im) pair, the
+// operand shape of the packed FP32 instructions (wd_df2.cuh).
+__device__ __forceinline__ dfc df_from_f4(float4 v) { return dfc{{v.x, v.z}, {v.y, v.w}}; }
 __device__ __forceinline__ float4 df_to_f4(dfc a)
 {
     const dfr re = df_norm(a.re), im = df_norm(a.im);
-    return make_float4(re.h, re.l, im.h, im.l);
+    return make_float4(re.h, im.h, re.l, im.l);
 }
 
 __host__ __device__ __forceinline__ dfr df_split(double x)
@@ -122,9 +124,9 @@ __device__ __forceinline__ double df_value(dfr a) { return (double)a.h + (double
 __device__ __forceinline__ float4 df_pack(double2 v)
 {
     const dfr r = df_split(v.x), i = df_split(v.y);
-    return make_float4(r.h, r.l, i.h, i.l);
+    return make_float4(r.h, i.h, r.l, i.l);
 }
 __device__ __forceinline__ double2 df_unpack(float4 v)
 {
-    return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    return make_double2((double)v.x + (double)v.z, (double)v.y + (double)v.w);
 }

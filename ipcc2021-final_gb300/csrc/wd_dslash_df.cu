@@ -1,7 +1,7 @@
 // wd_dslash_df.cu -- double-float (df64) hopping kernel.
 //
 // Same algorithm and memory traffic as the FP64 kernel (1536 B per output
-// site: every complex number is a 16-byte float4 {re.h, re.l, im.h, im.l}),
+// site: every complex number is a 16-byte float4 {re.h, im.h, re.l, im.l}),
 // with the arithmetic moved from the FP64 pipe to the FP32 pipe
 // (wd_df.cuh): ~8.5k FP32 operations per site instead of ~890 FP64 ones.
 // Results agree with FP64 to ~1e-14 relative L2 (storage rounding 2^-49,
@@ -16,6 +16,7 @@
 // holds 10 sites (lanes 0-9 colour 0, 10-19 colour 1, 20-29 colour 2).
 #include "wd_hop.cuh"
 #include "wd_df.cuh"
+#include "wd_df2.cuh"
 #include "wd_kernels.h"
 #include <type_traits>
 #include "wd_tune.h"
@@ -188,6 +189,139 @@ __global__ void __launch_bounds__(32 * WARPS) k_hop_df_pipe(const SplitDF p)
     }
 }
 
+// Packed form (wd_df2.cuh): the same colour-split, software-pipelined
+// kernel with every double-float operation issued on (re, im) pairs -- half
+// the arithmetic instructions for the same FP32-pipe work, bit-identical
+// results.
+struct DirLoadP {
+    dfp s[4];
+    dfp w[3];
+};
+
+__device__ __forceinline__ dfp ldp(const float4 *p, size_t i, bool on)
+{
+    return on ? dfp_from_f4(p[i]) : c_zero(dfp());
+}
+
+__device__ __forceinline__ dfp shfl_dfp(const dfp &v, int src)
+{
+    return dfp{make_float2(__shfl_sync(kFull, v.h.x, src), __shfl_sync(kFull, v.h.y, src)),
+               make_float2(__shfl_sync(kFull, v.l.x, src), __shfl_sync(kFull, v.l.y, src))};
+}
+
+template <int MU, bool FWD>
+__device__ __forceinline__ void pair_load(const SplitDF &p, const SplitCtx &x, DirLoadP &L)
+{
+    const size_t Vh = p.g.Vh;
+    const int nb = wd_neighbour(p.g, x.s, x.cs, MU, FWD);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) L.s[k] = ldp(p.in, (size_t)(k * 3 + x.col) * Vh + nb, x.on);
+    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? x.s : nb);
+    if constexpr (FWD) {
+        L.w[0] = ldp(gb, (size_t)(x.col * 3 + x.col) * Vh, x.on);
+        L.w[1] = ldp(gb, (size_t)(x.col * 3 + x.c1) * Vh, x.on);
+        L.w[2] = ldp(gb, (size_t)(x.col * 3 + x.c2) * Vh, x.on);
+    } else {
+        L.w[0] = ldp(gb, (size_t)(x.col * 3 + x.col) * Vh, x.on);
+        L.w[1] = ldp(gb, (size_t)(x.c1 * 3 + x.col) * Vh, x.on);
+        L.w[2] = ldp(gb, (size_t)(x.c2 * 3 + x.col) * Vh, x.on);
+    }
+}
+
+template <int MU, bool FWD, bool DAG>
+__device__ __forceinline__ void pair_compute(const SplitCtx &x, const DirLoadP &L, dfp *acc)
+{
+    constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
+    dfp h0, h1;
+    wd_proj1<MU, SG>(L.s[0], L.s[1], L.s[2], L.s[3], h0, h1);
+    const dfp h0b = shfl_dfp(h0, x.src1), h1b = shfl_dfp(h1, x.src1);
+    const dfp h0c = shfl_dfp(h0, x.src2), h1c = shfl_dfp(h1, x.src2);
+    dfp t0, t1;
+    if constexpr (FWD) {
+        t0 = c_madd(c_madd(c_mul(L.w[0], h0), L.w[1], h0b), L.w[2], h0c);
+        t1 = c_madd(c_madd(c_mul(L.w[0], h1), L.w[1], h1b), L.w[2], h1c);
+    } else {
+        t0 = c_maddc(c_maddc(c_mulc(L.w[0], h0), L.w[1], h0b), L.w[2], h0c);
+        t1 = c_maddc(c_maddc(c_mulc(L.w[0], h1), L.w[1], h1b), L.w[2], h1c);
+    }
+    wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
+}
+
+template <int MU, bool FWD, bool DAG>
+__device__ __forceinline__ void pair_dir(const SplitDF &p, const SplitCtx &x, dfp *acc)
+{
+    DirLoadP L;
+    pair_load<MU, FWD>(p, x, L);
+    pair_compute<MU, FWD, DAG>(x, L, acc);
+}
+
+// PIPE: loads of the next direction issued before the current one's arithmetic
+template <bool DAG, int WARPS, bool PIPE>
+__device__ __forceinline__ void hop_df_pair_body(const SplitDF &p)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int cq = lane / kSitesPerWarp;
+    const int ls = lane - cq * kSitesPerWarp;
+    const int s_raw = (blockIdx.x * WARPS + warp) * kSitesPerWarp + ls;
+    SplitCtx x;
+    x.on = cq < 3 && s_raw < p.g.Vh;
+    x.col = cq < 3 ? cq : 0;
+    x.s = x.on ? s_raw : 0;
+    x.c1 = x.col == 2 ? 0 : x.col + 1;
+    x.c2 = x.col == 0 ? 2 : x.col - 1;
+    x.src1 = ls + kSitesPerWarp * x.c1;
+    x.src2 = ls + kSitesPerWarp * x.c2;
+    x.cs = wd_site(p.g, x.s, p.cb);
+    dfp acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfp());
+    if constexpr (PIPE) {
+        DirLoadP A, B;
+        pair_load<0, true>(p, x, A);
+        pair_load<0, false>(p, x, B);
+        pair_compute<0, true, DAG>(x, A, acc);
+        pair_load<1, true>(p, x, A);
+        pair_compute<0, false, DAG>(x, B, acc);
+        pair_load<1, false>(p, x, B);
+        pair_compute<1, true, DAG>(x, A, acc);
+        pair_load<2, true>(p, x, A);
+        pair_compute<1, false, DAG>(x, B, acc);
+        pair_load<2, false>(p, x, B);
+        pair_compute<2, true, DAG>(x, A, acc);
+        pair_load<3, true>(p, x, A);
+        pair_compute<2, false, DAG>(x, B, acc);
+        pair_load<3, false>(p, x, B);
+        pair_compute<3, true, DAG>(x, A, acc);
+        pair_compute<3, false, DAG>(x, B, acc);
+    } else {
+        pair_dir<0, true, DAG>(p, x, acc);
+        pair_dir<0, false, DAG>(p, x, acc);
+        pair_dir<1, true, DAG>(p, x, acc);
+        pair_dir<1, false, DAG>(p, x, acc);
+        pair_dir<2, true, DAG>(p, x, acc);
+        pair_dir<2, false, DAG>(p, x, acc);
+        pair_dir<3, true, DAG>(p, x, acc);
+        pair_dir<3, false, DAG>(p, x, acc);
+    }
+    if (!x.on) return;
+    const size_t Vh = p.g.Vh;
+    const dfp al{make_float2(p.alpha.h, p.alpha.h), make_float2(p.alpha.l, p.alpha.l)};
+    const dfp be{make_float2(p.beta.h, p.beta.h), make_float2(p.beta.l, p.beta.l)};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const size_t i = (size_t)(k * 3 + x.col) * Vh + x.s;
+        dfp r = df_mul2(al, acc[k]);
+        if (p.x) r = df_madd2(r, be, dfp_from_f4(p.x[i]));
+        p.out[i] = dfp_to_f4(r);
+    }
+}
+
+template <bool DAG, int WARPS, bool PIPE>
+__global__ void __launch_bounds__(32 * WARPS) k_hop_df_pair(const SplitDF p)
+{
+    hop_df_pair_body<DAG, WARPS, PIPE>(p);
+}
+
 template <bool DAG, int WARPS, int MINB>
 __global__ void __launch_bounds__(32 * WARPS, MINB) k_hop_df_split(const SplitDF p)
 {
@@ -279,15 +413,31 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
         WD_LAUNCHED(ctx);
         return WD_OK;
     };
-    // variants: 4 warps/block; 2; 8; 4 warps with 6 blocks per SM (80 registers);
-    // software-pipelined with 4 and 2 warps per block
-    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 6, [&](int v) -> wd_status {
-        if (v == 1) return run(std::integral_constant<int, 2>(), std::integral_constant<int, 1>());
-        if (v == 2) return run(std::integral_constant<int, 8>(), std::integral_constant<int, 1>());
-        if (v == 3) return run(std::integral_constant<int, 4>(), std::integral_constant<int, 6>());
-        if (v == 4) return run_pipe(std::integral_constant<int, 4>());
-        if (v == 5) return run_pipe(std::integral_constant<int, 2>());
-        return run(std::integral_constant<int, 4>(), std::integral_constant<int, 1>());
+    auto run_pair = [&](auto warps, auto minb, auto pipe) -> wd_status {
+        constexpr int W = decltype(warps)::value, M = decltype(minb)::value;
+        constexpr bool PP = decltype(pipe)::value;
+        const int sites_per_block = kSitesPerWarp * W;
+        const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
+        static_assert(M == 0, "packed variants run without an occupancy floor");
+        if (dag) k_hop_df_pair<true, W, PP><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        else k_hop_df_pair<false, W, PP><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
+    // variants (32^3x64, 24^3x48 on GB300 in brackets): software-pipelined with 2
+    // and 4 warps per block [0.150 ms at 24^3x48]; colour-split at <= 80
+    // registers (6 blocks of 4 warps per SM); packed (re, im) pairs, 2 warps,
+    // not pipelined [0.161 ms: 29 % fewer instructions but more exposed
+    // memory latency].  The unbounded colour-split form (242 registers, 12 %
+    // of warps active, 0.225 ms) and the pipelined packed form (0.180 ms) lost
+    // everywhere and were dropped.
+    using F = std::false_type;
+    using W2 = std::integral_constant<int, 2>;
+    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 4, [&](int v) -> wd_status {
+        if (v == 1) return run_pipe(std::integral_constant<int, 4>());
+        if (v == 2) return run(std::integral_constant<int, 4>(), std::integral_constant<int, 6>());
+        if (v == 3) return run_pair(W2(), std::integral_constant<int, 0>(), F());
+        return run_pipe(W2());
     });
 }
 

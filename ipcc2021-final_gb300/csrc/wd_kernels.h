@@ -42,7 +42,7 @@ wd_status wd_blas_cg_update(wd_context *ctx, double2 alpha, const double2 *p, co
 // y = a*x (real a)
 wd_status wd_blas_scale(wd_context *ctx, double a, const double2 *x, double2 *y, int64_t n);
 
-// ---- double-float (df64) storage: float4 {re.h, re.l, im.h, im.l} per complex
+// ---- double-float (df64) storage: float4 {re.h, im.h, re.l, im.l} per complex
 wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_block, float4 *out_block,
                     const float4 *x_block, int cb, int dag, double alpha, double beta);
 wd_status wd_convert_f64_to_df(wd_context *ctx, const double2 *in, float4 *out, int64_t n);

@@ -49,8 +49,8 @@ struct HDF {
     __device__ void store(int c, int s, double2 v) const { p[(size_t)c * Vh + s] = df_pack(v); }
     __device__ float2 load_f32(int c, int s) const
     {
-        const float4 v = p[(size_t)c * Vh + s];
-        return make_float2(__fadd_rn(v.x, v.y), __fadd_rn(v.z, v.w));
+        const float4 v = p[(size_t)c * Vh + s];  // {re.h, im.h, re.l, im.l}
+        return make_float2(__fadd_rn(v.x, v.z), __fadd_rn(v.y, v.w));
     }
     __device__ void add_f32(int c, int s, float2 v) const
     {
