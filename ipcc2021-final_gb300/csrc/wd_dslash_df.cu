@@ -138,6 +138,31 @@ __device__ __forceinline__ void split_compute(const SplitCtx &x, const DirLoad &
     wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
 }
 
+// L2 prefetch of one direction's operands (the addresses split_load reads):
+// no registers held, so the next direction's requests are in flight while
+// the current one computes.
+__device__ __forceinline__ void pf_l2(const float4 *a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
+
+template <int MU, bool FWD>
+__device__ __forceinline__ void split_prefetch(const SplitDF &p, const SplitCtx &x)
+{
+    if (!x.on) return;
+    const size_t Vh = p.g.Vh;
+    const int nb = wd_neighbour(p.g, x.s, x.cs, MU, FWD);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) pf_l2(p.in + (size_t)(k * 3 + x.col) * Vh + nb);
+    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? x.s : nb);
+    if constexpr (FWD) {
+        pf_l2(gb + (size_t)(x.col * 3 + x.col) * Vh);
+        pf_l2(gb + (size_t)(x.col * 3 + x.c1) * Vh);
+        pf_l2(gb + (size_t)(x.col * 3 + x.c2) * Vh);
+    } else {
+        pf_l2(gb + (size_t)(x.col * 3 + x.col) * Vh);
+        pf_l2(gb + (size_t)(x.c1 * 3 + x.col) * Vh);
+        pf_l2(gb + (size_t)(x.c2 * 3 + x.col) * Vh);
+    }
+}
+
 template <bool DAG, int WARPS>
 __global__ void __launch_bounds__(32 * WARPS) k_hop_df_pipe(const SplitDF p)
 {
@@ -255,8 +280,10 @@ __device__ __forceinline__ void pair_dir(const SplitDF &p, const SplitCtx &x, df
     pair_compute<MU, FWD, DAG>(x, L, acc);
 }
 
-// PIPE: loads of the next direction issued before the current one's arithmetic
-template <bool DAG, int WARPS, bool PIPE>
+// PIPE: loads of the next direction issued before the current one's
+// arithmetic (in registers); otherwise PF prefetches the next direction into
+// L2 instead (no registers held)
+template <bool DAG, int WARPS, bool PIPE, bool PF = false>
 __device__ __forceinline__ void hop_df_pair_body(const SplitDF &p)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -294,12 +321,19 @@ __device__ __forceinline__ void hop_df_pair_body(const SplitDF &p)
         pair_compute<3, true, DAG>(x, A, acc);
         pair_compute<3, false, DAG>(x, B, acc);
     } else {
+        if constexpr (PF) split_prefetch<0, false>(p, x);
         pair_dir<0, true, DAG>(p, x, acc);
+        if constexpr (PF) split_prefetch<1, true>(p, x);
         pair_dir<0, false, DAG>(p, x, acc);
+        if constexpr (PF) split_prefetch<1, false>(p, x);
         pair_dir<1, true, DAG>(p, x, acc);
+        if constexpr (PF) split_prefetch<2, true>(p, x);
         pair_dir<1, false, DAG>(p, x, acc);
+        if constexpr (PF) split_prefetch<2, false>(p, x);
         pair_dir<2, true, DAG>(p, x, acc);
+        if constexpr (PF) split_prefetch<3, true>(p, x);
         pair_dir<2, false, DAG>(p, x, acc);
+        if constexpr (PF) split_prefetch<3, false>(p, x);
         pair_dir<3, true, DAG>(p, x, acc);
         pair_dir<3, false, DAG>(p, x, acc);
     }
@@ -316,10 +350,10 @@ __device__ __forceinline__ void hop_df_pair_body(const SplitDF &p)
     }
 }
 
-template <bool DAG, int WARPS, bool PIPE>
+template <bool DAG, int WARPS, bool PIPE, bool PF = false>
 __global__ void __launch_bounds__(32 * WARPS) k_hop_df_pair(const SplitDF p)
 {
-    hop_df_pair_body<DAG, WARPS, PIPE>(p);
+    hop_df_pair_body<DAG, WARPS, PIPE, PF>(p);
 }
 
 template <bool DAG, int WARPS, int MINB>
@@ -413,30 +447,33 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
         WD_LAUNCHED(ctx);
         return WD_OK;
     };
-    auto run_pair = [&](auto warps, auto minb, auto pipe) -> wd_status {
-        constexpr int W = decltype(warps)::value, M = decltype(minb)::value;
-        constexpr bool PP = decltype(pipe)::value;
+    auto run_pair = [&](auto warps, auto pf) -> wd_status {
+        constexpr int W = decltype(warps)::value;
+        constexpr bool PF = decltype(pf)::value;
         const int sites_per_block = kSitesPerWarp * W;
         const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
-        static_assert(M == 0, "packed variants run without an occupancy floor");
-        if (dag) k_hop_df_pair<true, W, PP><<<blocks, 32 * W, 0, ctx->stream>>>(p);
-        else k_hop_df_pair<false, W, PP><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        if (dag) k_hop_df_pair<true, W, false, PF><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        else k_hop_df_pair<false, W, false, PF><<<blocks, 32 * W, 0, ctx->stream>>>(p);
         WD_LAUNCHED(ctx);
         return WD_OK;
     };
-    // variants (32^3x64, 24^3x48 on GB300 in brackets): software-pipelined with 2
-    // and 4 warps per block [0.150 ms at 24^3x48]; colour-split at <= 80
-    // registers (6 blocks of 4 warps per SM); packed (re, im) pairs, 2 warps,
-    // not pipelined [0.161 ms: 29 % fewer instructions but more exposed
-    // memory latency].  The unbounded colour-split form (242 registers, 12 %
-    // of warps active, 0.225 ms) and the pipelined packed form (0.180 ms) lost
-    // everywhere and were dropped.
+    // variants (ncu at 24^3x48 on GB300 in brackets): software-pipelined with 2
+    // and 4 warps per block [0.150 ms, 123.5 M warp instructions, 55 % FMA
+    // pipe, 68 % issue]; colour-split at <= 80 registers (6 blocks of 4 warps
+    // per SM); packed (re, im) pairs, 2 warps [0.163 ms: 87.7 M instructions
+    // but 6.6 long-scoreboard stalls per issue]; packed pairs with an L2
+    // prefetch of the next direction [0.153 ms, 100.9 M, stalls 3.5].  Every
+    // form tried lands at ~55 % of the FMA pipe.  Dropped: the unbounded
+    // colour-split form (242 registers, 0.225 ms), the register-prefetching
+    // packed form (0.180 ms), L2 prefetch on the scalar form (0.161 ms).
     using F = std::false_type;
+    using T = std::true_type;
     using W2 = std::integral_constant<int, 2>;
-    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 4, [&](int v) -> wd_status {
+    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 5, [&](int v) -> wd_status {
         if (v == 1) return run_pipe(std::integral_constant<int, 4>());
         if (v == 2) return run(std::integral_constant<int, 4>(), std::integral_constant<int, 6>());
-        if (v == 3) return run_pair(W2(), std::integral_constant<int, 0>(), F());
+        if (v == 3) return run_pair(W2(), F());
+        if (v == 4) return run_pair(W2(), T());
         return run_pipe(W2());
     });
 }
