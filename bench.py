@@ -225,20 +225,25 @@ def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10, plans=SOLVE
     return out
 
 
-def batch_bench(wd, ctx) -> dict:
+def batch_bench(wd, ctx, profile: bool = False) -> dict:
     """Batched solves against the same systems solved one at a time.
     (a) one 24^3x48 lattice (seed 3, mass 0.05): 12 point sources (unit delta at
         site 0 for each spin/colour) + 12 Gaussian sources;
     (b) 16 lattices, L in {8,12,16,24} (four each), T = 2L, independent seeds,
         masses uniform in [0.05, 0.2], one Gaussian source each.
-    All to FP64 true residual 1e-10 with the mixed FP32 solver."""
-    import time as _t
+    All to FP64 true residual 1e-10 with the mixed FP32 solver.  profile=True
+    brackets each timed batched solve with cudaProfilerStart/Stop."""
+    import torch
 
-    def run(systems, params):
+    def run(systems, params, timed=False):
         for _, _, x, _ in systems:
             x.zero()
         ctx.sync()
+        if profile and timed:
+            torch.cuda.profiler.start()
         stats = ctx.solve_batch(systems, params)
+        if profile and timed:
+            torch.cuda.profiler.stop()
         assert all(st.converged and st.true_residual <= 1e-10 for st in stats)
         return stats[0].seconds, stats   # the solve; the FP64 check of each result follows it
 
@@ -268,7 +273,7 @@ def batch_bench(wd, ctx) -> dict:
     for name, rel in (("f32_inner_f64_reliable", wd.F64), ("f32_inner_df64_reliable", wd.DF64)):
         p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=rel)
         run(systems, p)  # warm-up
-        dt, stats = run(systems, p)
+        dt, stats = run(systems, p, timed=True)
         res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt,
                      "max_iterations": max(st.iterations for st in stats),
                      "max_true_residual": max(st.true_residual for st in stats)}
@@ -292,7 +297,7 @@ def batch_bench(wd, ctx) -> dict:
     res = {}
     p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=wd.F64)
     run(systems, p)
-    dt, stats = run(systems, p)
+    dt, stats = run(systems, p, timed=True)
     res["batched"] = {"seconds": dt, "solves_per_s": len(systems) / dt,
                       "iterations": [st.iterations for st in stats],
                       "max_true_residual": max(st.true_residual for st in stats)}
@@ -553,7 +558,7 @@ def run_ours(args) -> None:
                                                    plans=args.solver_plans, profile=args.profile_solves)}
             slat.close()
         if not args.no_batch:
-            line["batch"] = batch_bench(wd, ctx)
+            line["batch"] = batch_bench(wd, ctx, profile=args.profile_batch)
         if args.serve_requests > 0:
             line["serving"] = serve_bench(wd, ctx, args.serve_requests, args.serve_rates, args.serve_rates_f64,
                                           args.serve_requests_f64)
@@ -579,6 +584,8 @@ def main() -> None:
     ap.add_argument("--solver-plans", nargs="*", choices=SOLVER_PLANS, default=list(SOLVER_PLANS))
     ap.add_argument("--profile-solves", action="store_true",
                     help="bracket each timed solve with cudaProfilerStart/Stop (ncu --profile-from-start off)")
+    ap.add_argument("--profile-batch", action="store_true",
+                    help="bracket each timed batched solve with cudaProfilerStart/Stop")
     ap.add_argument("--solver-dims", type=int, nargs=4, default=[32, 32, 32, 64],
                     help="lattice of the second solver measurement (mixed-precision configuration; 48 48 48 96 also)")
     ap.add_argument("--solver-mass", type=float, default=0.01)

@@ -84,11 +84,12 @@ def test_bad_dims_and_mismatch(wd, ctx):
 
 
 @pytest.mark.parametrize("dims,dag,cb", [((16, 16, 16, 16), 0, 0), ((24, 24, 24, 32), 1, 1),
-                                         ((32, 32, 32, 32), 0, 1)])
+                                         ((32, 32, 32, 32), 0, 1), ((32, 32, 32, 64), 1, 0)])
 def test_host_offd_pipelined_large(wd, ctx, oracle, dims, dag, cb):
     """The host-buffer DslashoffdNew in one piece (16^4) and as overlapped
-    time-slab chunks (3 chunks at 24^3x32, 8 at 32^4); the untouched parity
-    of dest must come back zero whatever it held before."""
+    time-slab chunks (3 chunks at 24^3x32, 8 at 32^4, 16 chunks and 32 upload
+    units at 32^3x64); the untouched parity of dest must come back zero
+    whatever it held before."""
     gauge = wd.gen_gauge(dims, seed=5)
     src = wd.gen_source(dims, seed=5)
     out = np.full_like(src, np.nan + 1j)
