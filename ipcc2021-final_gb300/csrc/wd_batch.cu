@@ -5,11 +5,12 @@
 // Layout of a batch: systems are grouped by lattice (a group = one gauge
 // field + the right-hand sides that use it).  A batched operator launch
 // covers every group: blockIdx.x walks the groups' sites (a block table maps
-// blocks to groups), blockIdx.y selects up to kSysPerBlock systems of the
-// group.  Inside a block a warp holds 32 consecutive sites of one system,
-// so spinor loads stay coalesced, and the kSysPerBlock warps that share a
-// site range read the same links, which DRAM delivers once and L1 serves to
-// the rest: link traffic is divided by the number of right-hand sides.
+// blocks to groups), blockIdx.y selects up to SYS systems of the group (SYS
+// and the occupancy bound are tuned launch variants).  Inside a block a warp
+// holds 32 consecutive sites of one system, so spinor loads stay coalesced,
+// and the SYS warps that share a site range read the same links, which DRAM
+// delivers once and L1 serves to the rest: link traffic is divided by the
+// number of right-hand sides.
 //
 // Per-system scalars (rr, |t|^2, alpha, beta, active) live in device memory.
 // One CG iteration (4 batched hops, per-system reductions, scalar update,
@@ -24,18 +25,20 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <type_traits>
 #include <vector>
 #include "wd_df.cuh"
 #include "wd_hop.cuh"
 #include "wd_lp.cuh"
 #include "wd_reduce.cuh"
 #include "wd_solver.h"
+#include "wd_tune.h"
 
 namespace {
 
-constexpr int kSites = 32;       // sites per warp (one system per warp)
-constexpr int kSysPerBlock = 8;  // warps (systems) per block
+constexpr int kSites = 32;  // sites per warp (one system per warp)
 constexpr int kChunk = 8192;     // sites per reduction chunk (one block each)
+constexpr int kBatchHopVariants = 5;
 
 struct BGroup {
     WdGeom g;
@@ -92,12 +95,15 @@ __device__ __forceinline__ int find_group(const BGroup *groups, int ngroups, int
     return lo;
 }
 
-template <bool DAG, bool F16>
-__global__ void __launch_bounds__(kSites * kSysPerBlock) k_batch_hop(const BTable t)
+// SYS systems (warps) per block sharing the block's sites; MINB blocks per SM
+// (0: no bound) bound the registers (the kernel is latency-bound: DRAM bytes per
+// system-site sit at the link-shared minimum, so occupancy sets its speed)
+template <bool DAG, bool F16, int SYS, int MINB>
+__global__ void __launch_bounds__(kSites * SYS, MINB) k_batch_hop(const BTable t)
 {
     const int gi = find_group(t.groups, t.ngroups, blockIdx.x);
     const BGroup &G = t.groups[gi];
-    const int r = blockIdx.y * kSysPerBlock + (threadIdx.x / kSites);
+    const int r = blockIdx.y * SYS + (threadIdx.x / kSites);
     const int s = (blockIdx.x - G.block_start) * kSites + (threadIdx.x % kSites);
     if (r >= G.nsys || s >= G.g.Vh) return;
     const int sys = G.first_sys + r;
@@ -386,7 +392,8 @@ class BatchEngine {
     DevArray<double> d_rr_, d_tt_, d_partial_;
     DevArray<float> d_a_, d_b_;
     DevArray<int> d_active_, d_chunk_sys_;
-    int grid_x_ = 0, grid_y_ = 1, nchunks_ = 0, ngroups_ = 0;
+    int grid_x_ = 0, nchunks_ = 0, ngroups_ = 0, max_group_sys_ = 1;
+    int hop_variant_ = 0;  // launch shape of the batched hop (tuned in rebuild)
     cudaGraphExec_t exec_ = nullptr;
     uint64_t kernels_per_graph_ = 0;
 
@@ -399,6 +406,7 @@ class BatchEngine {
     wd_status finish(EngineSys &s);
     wd_status rebuild();
     wd_status iteration(const BState &bst);
+    wd_status hop(int h, int cb, int dag, int variant);
     wd_status upload_scalars();
 };
 
@@ -533,8 +541,8 @@ wd_status BatchEngine::rebuild()
         groups.back().nsys++;
     }
     grid_x_ = blocks;
-    grid_y_ = 1;
-    for (const BGroup &G : groups) grid_y_ = std::max(grid_y_, (G.nsys + kSysPerBlock - 1) / kSysPerBlock);
+    max_group_sys_ = 1;
+    for (const BGroup &G : groups) max_group_sys_ = std::max(max_group_sys_, G.nsys);
     ngroups_ = (int)groups.size();
     std::vector<BVec> bvec(nsys);
     std::vector<int> chunk_sys;
@@ -584,6 +592,20 @@ wd_status BatchEngine::rebuild()
     if ((st = d_partial_.put(ctx_, zeros_p)) != WD_OK) return st;
     if ((st = d_chunk_sys_.put(ctx_, chunk_sys)) != WD_OK) return st;
 
+    // launch shape of the batched hop, timed on its first operator (p -> the
+    // odd scratch, which every iteration rewrites before reading) outside the
+    // capture; keyed by precision and the batch's system-sites to a power of 2
+    int64_t sites = 0;
+    for (const BGroup &G : groups) sites += (int64_t)G.g.Vh * G.nsys;
+    int bucket = 1;
+    while ((int64_t)bucket < sites && bucket < (1 << 30)) bucket <<= 1;
+    if ((st = wd_tune_launch(ctx_, f16 ? "batch_hop_f16" : "batch_hop_f32", bucket, kBatchHopVariants,
+                             [&](int v) -> wd_status {
+                                 hop_variant_ = v;
+                                 return hop(0, 1, 0, v);
+                             })) != WD_OK)
+        return st;
+
     // capture per_graph iterations
     const BState bst{d_rr_.p, d_tt_.p, d_a_.p, d_b_.p, d_active_.p, d_partial_.p, d_chunk_sys_.p, nchunks_};
     const uint64_t before = ctx_->launches;
@@ -609,27 +631,45 @@ wd_status BatchEngine::rebuild()
     return WD_OK;
 }
 
-wd_status BatchEngine::iteration(const BState &bst)
+// batched hop h (operand table h) with launch variant v: (systems per block,
+// min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12), (4, none)
+wd_status BatchEngine::hop(int h, int cb, int dag, int v)
 {
-    const int nsys = (int)sys_.size();
-    const bool f16 = L_ == WD_PREC_F16;
-    auto hop = [&](int h, int cb, int dag) -> wd_status {
-        const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_active_.p, cb};
-        dim3 grid(grid_x_, grid_y_);
-        const int threads = kSites * kSysPerBlock;
-        if (f16) {
-            if (dag) k_batch_hop<true, true><<<grid, threads, 0, ctx_->stream>>>(t);
-            else k_batch_hop<false, true><<<grid, threads, 0, ctx_->stream>>>(t);
+    const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_active_.p, cb};
+    auto run = [&](auto sys, auto minb) -> wd_status {
+        constexpr int S = decltype(sys)::value, M = decltype(minb)::value;
+        const dim3 grid(grid_x_, (max_group_sys_ + S - 1) / S);
+        if (L_ == WD_PREC_F16) {
+            if (dag) k_batch_hop<true, true, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+            else k_batch_hop<false, true, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
         } else {
-            if (dag) k_batch_hop<true, false><<<grid, threads, 0, ctx_->stream>>>(t);
-            else k_batch_hop<false, false><<<grid, threads, 0, ctx_->stream>>>(t);
+            if (dag) k_batch_hop<true, false, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+            else k_batch_hop<false, false, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
         }
         WD_LAUNCHED(ctx_);
         return WD_OK;
     };
+    using I2 = std::integral_constant<int, 2>;
+    using I4 = std::integral_constant<int, 4>;
+    using I8 = std::integral_constant<int, 8>;
+    using I0 = std::integral_constant<int, 0>;
+    switch (v) {
+    case 1: return run(I8(), std::integral_constant<int, 3>());
+    case 2: return run(I4(), std::integral_constant<int, 6>());
+    case 3: return run(I2(), std::integral_constant<int, 12>());
+    case 4: return run(I4(), I0());
+    default: return run(I8(), I0());
+    }
+}
+
+wd_status BatchEngine::iteration(const BState &bst)
+{
+    const int nsys = (int)sys_.size();
+    const bool f16 = L_ == WD_PREC_F16;
+    const int v = hop_variant_;
     wd_status e;
-    if ((e = hop(0, 1, 0)) != WD_OK || (e = hop(1, 0, 0)) != WD_OK) return e;  // t = Mhat p
-    if ((e = hop(2, 1, 1)) != WD_OK || (e = hop(3, 0, 1)) != WD_OK) return e;  // q = Mhat^dag t
+    if ((e = hop(0, 1, 0, v)) != WD_OK || (e = hop(1, 0, 0, v)) != WD_OK) return e;  // t = Mhat p
+    if ((e = hop(2, 1, 1, v)) != WD_OK || (e = hop(3, 0, 1, v)) != WD_OK) return e;  // q = Mhat^dag t
     if (f16) k_batch_norm_t<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
     else k_batch_norm_t<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
     WD_LAUNCHED(ctx_);
