@@ -99,3 +99,23 @@ def test_host_offd_pipelined_large(wd, ctx, oracle, dims, dag, cb):
     assert rel_l2(out, ref) < TOL
     half = src.size // 2
     assert np.all(out[(1 - cb) * half:(2 - cb) * half] == 0)
+
+
+def test_volume_beyond_32bit_byte_offsets(wd, ctx, oracle):
+    """32x32x32x128 (4.2M sites): the FP64 links (2.4 GB) and their double-float
+    copy lie beyond 2^31 bytes, so every plane offset must be computed in 64
+    bits.  Hopping terms in every storage against the oracle (bars: 1e-13 for
+    FP64 and double-float, 2e-6 FP32, 5e-3 FP16), both parities and dagger."""
+    dims = (32, 32, 32, 128)
+    gauge = wd.gen_gauge(dims, seed=9)
+    src = wd.gen_source(dims, seed=9)
+    lat = ctx.lattice(dims, gauge)
+    want = {(dag, cb): oracle.dslash_offd(src, gauge, dims, dag, cb) for dag, cb in ((0, 0), (1, 1))}
+    for prec, bar in ((wd.F64, TOL), (wd.DF64, TOL), (wd.F32, 2e-6), (wd.F16, 5e-3)):
+        fi, fo = lat.field(src, prec=prec), lat.field(prec=prec)
+        for (dag, cb), ref in want.items():
+            lat.dslash_offd(fi, fo, dag, cb, prec)
+            assert rel_l2(fo.download(), ref) < bar, (prec, dag, cb)
+        fi.close()
+        fo.close()
+    lat.close()
