@@ -6,12 +6,52 @@
 // Arithmetic: 1320 flop per site.  On GB300 the FP64 pipe (~1.2 TFLOP/s
 // measured) rather than HBM bounds this kernel; wd_dslash_df.cu holds the
 // double-float variant that moves the arithmetic onto the FP32 pipe.
+#include <cmath>
+#include <cstdint>
 #include "wd_hop.cuh"
 #include "wd_kernels.h"
 #include <type_traits>
 #include "wd_tune.h"
 
 namespace {
+
+// Output scaling without the FP64 pipe when alpha is 1 or a power of two
+// (DslashoffdNew's -1/2, the Schur operator's first hop's 1): a power-of-two
+// factor only moves the exponent, so integer arithmetic on the bits gives
+// the FP64 product exactly; zeros, subnormal results and non-finite values
+// take the FP64 multiply.  24 fewer FP64 operations per site (of ~890).
+struct F64Scale {
+    double alpha;
+    int mode;       // 0: multiply, 1: identity, 2: exponent shift
+    int shift;      // mode 2: alpha = sign * 2^shift
+    uint64_t sign;  // mode 2: sign bit of alpha
+
+    static F64Scale make(double a)
+    {
+        F64Scale f{a, 0, 0, 0};
+        int e = 0;
+        const double m = std::frexp(a, &e);  // a = m * 2^e, |m| in [0.5, 1)
+        if (a == 1.0) f.mode = 1;
+        else if (std::fabs(m) == 0.5 && e - 1 > -1000 && e - 1 < 1000) {
+            f.mode = 2;
+            f.shift = e - 1;
+            f.sign = a < 0 ? 0x8000000000000000ull : 0ull;
+        }
+        return f;
+    }
+    __device__ __forceinline__ double apply(double v) const
+    {
+        if (mode == 1) return v;
+        if (mode == 2) {
+            const uint64_t b = (uint64_t)__double_as_longlong(v);
+            const int ex = (int)((b >> 52) & 0x7ff);
+            if (ex > 0 && ex < 0x7ff && ex + shift > 0 && ex + shift < 0x7ff)
+                return __longlong_as_double((long long)((b + ((uint64_t)(int64_t)shift << 52)) ^ sign));
+        }
+        return v * alpha;
+    }
+    __device__ __forceinline__ double2 apply(double2 v) const { return make_double2(apply(v.x), apply(v.y)); }
+};
 
 template <int THREADS>
 struct HopF64 {
@@ -24,6 +64,7 @@ struct HopF64 {
     const double2 *__restrict__ x;      // parity cb block or null
     double2 *__restrict__ out;          // parity cb block
     double alpha, beta;
+    F64Scale scale;                     // alpha, applied when there is no x
 
     __device__ __forceinline__ void load_in(int s, C *v) const
     {
@@ -44,7 +85,7 @@ struct HopF64 {
                 out[(size_t)c * g.Vh + s] = c_axpby(alpha, acc[c], beta, x[(size_t)c * g.Vh + s]);
         } else {
 #pragma unroll
-            for (int c = 0; c < 12; ++c) out[(size_t)c * g.Vh + s] = c_scale(acc[c], alpha);
+            for (int c = 0; c < 12; ++c) out[(size_t)c * g.Vh + s] = scale.apply(acc[c]);
         }
     }
 };
@@ -68,7 +109,7 @@ struct HopF64AoS : HopF64<THREADS> {
     {
         double2 *o = this->out + (size_t)s * 12;
 #pragma unroll
-        for (int c = 0; c < 12; ++c) o[c] = c_scale(acc[c], this->alpha);
+        for (int c = 0; c < 12; ++c) o[c] = this->scale.apply(acc[c]);
     }
 };
 
@@ -87,6 +128,7 @@ wd_status wd_hop_f64_aos_range(wd_context *ctx, cudaStream_t stream, const wd_la
     p.out = out_aos;
     p.alpha = alpha;
     p.beta = 0.0;
+    p.scale = F64Scale::make(alpha);
     const int n = s_hi - s_lo;
     if (n <= 0) return WD_OK;
     const int blocks = (n + P::kThreads - 1) / P::kThreads;
@@ -111,6 +153,7 @@ wd_status wd_hop_f64(wd_context *ctx, const wd_lattice *lat, const double2 *in_b
         p.out = out_block;
         p.alpha = alpha;
         p.beta = beta;
+        p.scale = F64Scale::make(alpha);
         const int blocks = (lat->g.Vh + P::kThreads - 1) / P::kThreads;
         if (dag) wd_hop_kernel<true><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
         else wd_hop_kernel<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
@@ -138,6 +181,7 @@ wd_status wd_hop_f64_range(wd_context *ctx, cudaStream_t stream, const wd_lattic
     p.out = out_block;
     p.alpha = alpha;
     p.beta = 0.0;
+    p.scale = F64Scale::make(alpha);
     const int n = s_hi - s_lo;
     if (n <= 0) return WD_OK;
     const int blocks = (n + P::kThreads - 1) / P::kThreads;
