@@ -9,6 +9,7 @@ __device__ __forceinline__ double2 c_zero(double2) { return make_double2(0.0, 0.
 __device__ __forceinline__ double2 c_add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 c_sub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 c_i(double2 a) { return make_double2(-a.y, a.x); }
+__device__ __forceinline__ double2 c_neg(double2 a) { return make_double2(-a.x, -a.y); }
 __device__ __forceinline__ double2 c_scale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 // u * h
 __device__ __forceinline__ double2 c_mul(double2 u, double2 h)
@@ -50,6 +51,7 @@ __device__ __forceinline__ float2 c_zero(float2) { return make_float2(0.f, 0.f);
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 c_i(float2 a) { return make_float2(-a.y, a.x); }
+__device__ __forceinline__ float2 c_neg(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 __device__ __forceinline__ float2 c_mul(float2 u, float2 h)
 {

@@ -75,6 +75,35 @@ __device__ __forceinline__ void wd_recon1(const C &t0, const C &t1, C &d0, C &d1
     }
 }
 
+// wd_recon1 for the first direction, into zero accumulators: assignments
+// instead of additions to zero (24 fewer adds per site; a result can differ
+// only in the sign of a zero)
+template <int X, class C>
+__device__ __forceinline__ C wd_sgv(const C &v)
+{
+    if constexpr (X > 0) return v;
+    else return c_neg(v);
+}
+template <int MU, int SG, class C>
+__device__ __forceinline__ void wd_recon1_first(const C &t0, const C &t1, C &d0, C &d1, C &d2, C &d3)
+{
+    d0 = t0;
+    d1 = t1;
+    if constexpr (MU == 0) {
+        d2 = wd_sgv<-SG>(c_i(t1));
+        d3 = wd_sgv<-SG>(c_i(t0));
+    } else if constexpr (MU == 1) {
+        d2 = wd_sgv<SG>(t1);
+        d3 = wd_sgv<-SG>(t0);
+    } else if constexpr (MU == 2) {
+        d2 = wd_sgv<-SG>(c_i(t0));
+        d3 = wd_sgv<SG>(c_i(t1));
+    } else {
+        d2 = wd_sgv<SG>(t0);
+        d3 = wd_sgv<SG>(t1);
+    }
+}
+
 // d + k t and d + k (i t), k real (FP32 complex only)
 __device__ __forceinline__ float2 wd_cfma(float k, float2 t, float2 d)
 {
@@ -122,8 +151,8 @@ __device__ __forceinline__ void wd_recon(const C *t0, const C *t1, C *acc)
     for (int a = 0; a < 3; ++a) wd_recon1<MU, SG>(t0[a], t1[a], acc[a], acc[3 + a], acc[6 + a], acc[9 + a]);
 }
 
-// One of the eight neighbour terms.
-template <int MU, bool FWD, bool DAG, class P>
+// One of the eight neighbour terms (FIRST: the accumulators hold zeros).
+template <int MU, bool FWD, bool DAG, class P, bool FIRST = false>
 __device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, typename P::C *acc)
 {
     using C = typename P::C;
@@ -165,6 +194,9 @@ __device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, t
     if constexpr (kScaled) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) wd_recon1_scaled<MU, SG>(t0[a], t1[a], sc, acc[a], acc[3 + a], acc[6 + a], acc[9 + a]);
+    } else if constexpr (FIRST) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) wd_recon1_first<MU, SG>(t0[a], t1[a], acc[a], acc[3 + a], acc[6 + a], acc[9 + a]);
     } else {
         wd_recon<MU, SG>(t0, t1, acc);
     }
@@ -177,7 +209,7 @@ __device__ __forceinline__ void wd_hop_site(const P &p, int s, typename P::C *ac
     const WdSite c = wd_site(p.g, s, p.cb);
 #pragma unroll
     for (int k = 0; k < 12; ++k) acc[k] = c_zero(C());
-    wd_hop_dir<0, true, DAG>(p, s, c, acc);
+    wd_hop_dir<0, true, DAG, P, true>(p, s, c, acc);
     wd_hop_dir<0, false, DAG>(p, s, c, acc);
     wd_hop_dir<1, true, DAG>(p, s, c, acc);
     wd_hop_dir<1, false, DAG>(p, s, c, acc);
