@@ -57,6 +57,7 @@ template <int THREADS>
 struct HopF64 {
     using C = double2;
     static constexpr int kThreads = THREADS;
+    static constexpr bool kPairDirs = true;  // FP64-pipe bound: fewest operations wins
     WdGeom g;
     int cb;
     const double2 *__restrict__ in;     // parity 1-cb block [12][Vh]
