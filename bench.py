@@ -183,6 +183,58 @@ def dslash_variants(wd, ctx, lat, src, stream, steps: int, vh: int, peak: float)
     return out
 
 
+def small_config_bench(wd, ctx, with_cpu: bool) -> dict:
+    """The reference's own CPU-runnable case: 8^3x16, seed 1, mass 0.1, CG to
+    1e-10 (max 1000 iterations).  On the GPU: the even-odd CG (relative true
+    residual) and the reference's CG recurrences (WD_SOLVER_CGNR_REF, absolute
+    stop on the normal residual), both from a zero initial guess.  With
+    with_cpu, the oracle's C restatement of the reference's CGinvert and
+    DslashoffdNew on ONE host thread (the reference runs one rank per core) on
+    the same inputs -- a baseline, not part of the GPU path."""
+    dims, mass = (8, 8, 8, 16), 0.1
+    gauge, src = wd.gen_gauge(dims, 1, EPS), wd.gen_source(dims, 1)
+    lat = ctx.lattice(dims, gauge)
+    b, x = lat.field(src), lat.field()
+    out = {"workload": "8x8x8x16 (8192 sites), seed 1, mass 0.1, CG to 1e-10, max 1000 iterations"}
+    for name, kind in (("gpu_cg_eo_f64", wd.CG_EO), ("gpu_cgnr_ref_f64", wd.CGNR_REF)):
+        p = wd.solver_params(kind=kind, mass=mass, tol=1e-10, max_iter=1000)
+        x.zero()
+        lat.solve(b, x, p)  # warm-up
+        x.zero()
+        st = lat.solve(b, x, p)
+        out[name] = {"seconds": st.seconds, "iterations": st.iterations, "true_residual": st.true_residual}
+    fi, fo = lat.field(src), lat.field()
+    n = 200
+    lat.dslash_offd(fi, fo, 0, 0)
+    ctx.sync()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        lat.dslash_offd(fi, fo, 0, 0)
+    ctx.sync()
+    out["gpu_dslashoffd_ms"] = (time.perf_counter() - t0) / n * 1e3
+    for f in (b, x, fi, fo):
+        f.close()
+    lat.close()
+    if with_cpu:
+        sys.path.insert(0, str(REPO / "oracle"))
+        from oracle import Oracle
+
+        orc = Oracle()
+        all_threads = orc.threads(os.cpu_count() or 1)
+        orc.threads(1)
+        t0 = time.perf_counter()
+        _, it, rsd = orc.cg_ref(src, gauge, dims, mass, 1000, 1e-10, np.zeros_like(src))
+        cg_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for _ in range(100):
+            orc.dslash_offd(src, gauge, dims, 0, 0)
+        ds_ms = (time.perf_counter() - t0) / 100 * 1e3
+        orc.threads(all_threads)
+        out["cpu_oracle_1_thread"] = {"cginvert_seconds": cg_s, "cginvert_iterations": it,
+                                      "dslashoffd_ms": ds_ms, "cores": 1, "kind": "port"}
+    return out
+
+
 SOLVER_PLANS = ("f64", "df64", "mixed_f32", "mixed_f16", "mixed_f16_df64")
 
 
@@ -557,6 +609,8 @@ def run_ours(args) -> None:
                                     **solver_bench(wd, ctx, slat, wd.gen_source(sd, SEED), args.solver_mass,
                                                    plans=args.solver_plans, profile=args.profile_solves)}
             slat.close()
+        if not args.no_solver:
+            line["small_config"] = small_config_bench(wd, ctx, not args.no_cpu_baseline)
         if not args.no_batch:
             line["batch"] = batch_bench(wd, ctx, profile=args.profile_batch)
         if args.serve_requests > 0:
