@@ -943,15 +943,19 @@ extern "C" wd_status wd_server_add_lattice(wd_server *sv, const int dims[4], con
     // derived link copies the server will use, built now so they count against the budget
     double bytes = (double)lat->volume * 4 * 9 * sizeof(double2);
     if (sv->cfg.prec != WD_PREC_F64) {
-        if ((st = wd_lattice_gauge_lp(sv->ctx, lat, sv->cfg.prec)) != WD_OK) return st;
+        st = wd_lattice_gauge_lp(sv->ctx, lat, sv->cfg.prec);
         bytes += (double)lat->volume * 4 * (sv->cfg.prec == WD_PREC_F16 ? 24 : 48);
-        if (sv->cfg.prec == WD_PREC_F16) {  // reliable updates apply Mhat^dag with FP32 links
-            if ((st = wd_lattice_gauge_lp(sv->ctx, lat, WD_PREC_F32)) != WD_OK) return st;
+        if (st == WD_OK && sv->cfg.prec == WD_PREC_F16) {  // reliable updates apply Mhat^dag with FP32 links
+            st = wd_lattice_gauge_lp(sv->ctx, lat, WD_PREC_F32);
             bytes += (double)lat->volume * 4 * 48;
         }
-        if (sv->cfg.prec_reliable == WD_PREC_DF64) {
-            if ((st = wd_lattice_gauge_df(sv->ctx, lat)) != WD_OK) return st;
+        if (st == WD_OK && sv->cfg.prec_reliable == WD_PREC_DF64) {
+            st = wd_lattice_gauge_df(sv->ctx, lat);
             bytes += (double)lat->volume * 4 * 9 * sizeof(float4);
+        }
+        if (st != WD_OK) {
+            wd_lattice_destroy(lat);
+            return st;
         }
     }
     sv->gauge_bytes += bytes;
