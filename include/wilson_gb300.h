@@ -280,6 +280,29 @@ wd_status wd_gen_gauge(const int dims[4], uint64_t seed, double eps, double *con
 /* Complex Gaussian source on V*12 entries, normalised to unit L2. */
 wd_status wd_gen_source(const int dims[4], uint64_t seed, double *src);
 
+/* ---- short names of the drop-in boundary -------------------------------- */
+/* Forwards to the entry points above: context, gauge upload (the reference
+ * layout of src/load_gauge.cpp:141-161 -> a resident lattice), fermion
+ * upload/download (eo*12 + spin*3 + colour), the full operator M
+ * (DslashNew, src/invert.cpp:138-156) in FP64, and CG. */
+wd_status wd_ctx_create(int device, wd_context **ctx);
+void wd_ctx_destroy(wd_context *ctx);
+wd_status wd_gauge_upload(wd_context *ctx, const double *const ref_layout[4], const int dims[4], wd_lattice **lat);
+wd_status wd_fermion_upload(wd_context *ctx, wd_field *f, const double *ref_layout);
+wd_status wd_fermion_download(wd_context *ctx, const wd_field *f, double *ref_layout);
+wd_status wd_M(wd_context *ctx, const wd_lattice *lat, const wd_field *in, wd_field *out, double mass, int dag);
+/* CG on the field's lattice.  flags: WD_CG_REFERENCE selects the reference's
+ * CG recurrences (CGinvert, src/invert.cpp:25-121) instead of the even-odd
+ * CG; bits 1-2 the inner precision (wd_precision << 1); WD_CG_RELIABLE_DF64
+ * double-float reliable updates; WD_CG_INITIAL_GUESS starts from dest. */
+enum {
+    WD_CG_REFERENCE = 1,
+    WD_CG_RELIABLE_DF64 = 8,
+    WD_CG_INITIAL_GUESS = 16
+};
+wd_status wd_cg(wd_context *ctx, const wd_lattice *lat, const wd_field *src, wd_field *dest, double mass, double tol,
+                int max_iter, int flags, wd_solver_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

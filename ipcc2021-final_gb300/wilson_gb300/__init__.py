@@ -59,6 +59,13 @@ def _load() -> C.CDLL:
     d4 = C.POINTER(C.c_void_p)
     sigs = {
         "wd_context_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
+        "wd_ctx_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
+        "wd_ctx_destroy": (None, [vp]),
+        "wd_gauge_upload": (C.c_int, [vp, d4, ip, C.POINTER(vp)]),
+        "wd_fermion_upload": (C.c_int, [vp, vp, vp]),
+        "wd_fermion_download": (C.c_int, [vp, vp, vp]),
+        "wd_M": (C.c_int, [vp, vp, vp, vp, C.c_double, C.c_int]),
+        "wd_cg": (C.c_int, [vp, vp, vp, vp, C.c_double, C.c_double, C.c_int, C.c_int, C.POINTER(SolverStats)]),
         "wd_context_destroy": (None, [vp]),
         "wd_status_string": (C.c_char_p, [C.c_int]),
         "wd_last_error": (C.c_char_p, [vp]),
