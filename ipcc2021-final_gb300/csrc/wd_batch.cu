@@ -39,6 +39,7 @@ namespace {
 constexpr int kSites = 32;  // sites per warp (one system per warp)
 constexpr int kChunk = 8192;     // sites per reduction chunk (one block each)
 constexpr int kBatchHopVariants = 5;
+constexpr int kRelGroup = WD_RED_SLOTS / 2;  // reliable updates per host wait
 
 struct BGroup {
     WdGeom g;
@@ -403,6 +404,7 @@ class BatchEngine {
         exec_ = nullptr;
     }
     wd_status reliable(EngineSys &s, bool reset_p, double *rr, double *ss);
+    wd_status reliable_enqueue(EngineSys &s, bool reset_p, int slot);
     wd_status finish(EngineSys &s);
     wd_status rebuild();
     wd_status iteration(const BState &bst);
@@ -422,11 +424,22 @@ static inline void slices(EngineSys &s, WdVec &b_e, WdVec &b_o, WdVec &x_e, WdVe
 // reliable update: x_e += x_s; s = bhat - Mhat x_e; r_s = Mhat^dag s (FP32); p <- r_s on a restart
 wd_status BatchEngine::reliable(EngineSys &s, bool reset_p, double *rr, double *ss)
 {
+    wd_status e = reliable_enqueue(s, reset_p, 0);
+    if (e != WD_OK) return e;
+    double2 red[2];
+    if ((e = wd_red_fetch(ctx_, 2, red)) != WD_OK) return e;
+    *rr = red[0].x;
+    *ss = red[1].x;
+    return WD_OK;
+}
+
+wd_status BatchEngine::reliable_enqueue(EngineSys &s, bool reset_p, int slot)
+{
     SysBufs &B = s.B;
     WdVec b_e, b_o, x_e, x_o;
     slices(s, b_e, b_o, x_e, x_o);
     const WdMxReliable rv{B.xs.v, x_e, B.bhat.v, B.t_h.v, B.s_e.v, B.tmp_oh.v, B.r_h.v, B.rs.v};
-    return wd_mx_reliable(ctx_, s.lat, s.mass, L_, H_, rv, reset_p ? &B.p.v : nullptr, rr, ss);
+    return wd_mx_reliable_enqueue(ctx_, s.lat, s.mass, L_, H_, rv, reset_p ? &B.p.v : nullptr, slot);
 }
 
 wd_status BatchEngine::add(int tag, const wd_lattice *lat, const double2 *src, double2 *dest, double mass,
@@ -722,6 +735,10 @@ wd_status BatchEngine::step(std::vector<int> *finished)
     std::vector<double> rr(nsys);
     WD_CUDA(ctx_, cudaMemcpyAsync(rr.data(), d_rr_.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, ctx_->stream));
     WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
+    // systems whose residual fell by delta (or reached the target) take a
+    // reliable update; the updates of up to kRelGroup systems are enqueued
+    // back to back and their norms fetched with one host wait
+    std::vector<int> upd;
     for (int k = 0; k < nsys; ++k) {
         EngineSys &s = *sys_[k];
         if (!s.active) continue;
@@ -729,10 +746,20 @@ wd_status BatchEngine::step(std::vector<int> *finished)
         const double rr_new = rr[k];
         if (!std::isfinite(rr_new)) return wd_fail(ctx_, WD_ERR_NAN, "batched CG residual is not finite");
         s.rr = rr_new;
-        const bool at_target = std::sqrt(rr_new) <= s.target;
-        if (rr_new < delta_ * delta_ * s.rr_max || at_target) {
-            double rrt, ss;
-            if ((st = reliable(s, false, &rrt, &ss)) != WD_OK) return st;
+        if (rr_new < delta_ * delta_ * s.rr_max || std::sqrt(rr_new) <= s.target) upd.push_back(k);
+        else if (s.iters >= max_iter_ && (st = finish(s)) != WD_OK)  // give up: return what it has
+            return st;
+    }
+    for (size_t g0 = 0; g0 < upd.size(); g0 += kRelGroup) {
+        const size_t g1 = std::min(upd.size(), g0 + kRelGroup);
+        for (size_t j = g0; j < g1; ++j)
+            if ((st = reliable_enqueue(*sys_[upd[j]], false, 2 * (int)(j - g0))) != WD_OK) return st;
+        double2 red[2 * kRelGroup];
+        if ((st = wd_red_fetch(ctx_, 2 * (int)(g1 - g0), red)) != WD_OK) return st;
+        for (size_t j = g0; j < g1; ++j) {
+            EngineSys &s = *sys_[upd[j]];
+            const double rrt = red[2 * (j - g0)].x, ss = red[2 * (j - g0) + 1].x;
+            const bool at_target = std::sqrt(s.rr) <= s.target;
             s.updates++;
             s.true_res = std::sqrt(ss) / s.norm_b;
             if (s.true_res <= s.tol) {
@@ -745,9 +772,7 @@ wd_status BatchEngine::step(std::vector<int> *finished)
             }
             s.rr = s.rr_max = rrt;  // continue from the recomputed residual
             scalars_dirty_ = true;
-        }
-        if (s.iters >= max_iter_) {  // give up on this system: return what it has
-            if ((st = finish(s)) != WD_OK) return st;
+            if (s.iters >= max_iter_ && (st = finish(s)) != WD_OK) return st;
         }
     }
     WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));

@@ -246,11 +246,11 @@ struct Mixed {
         WD_LAUNCHED(ctx);
         return WD_OK;
     }
-    wd_status norm2_f32(WdVec t) const
+    wd_status norm2_f32(WdVec t, int slot) const
     {
         k_mx_norm2<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(t, Vh), Vh, (double2 *)ctx->red_partial);
         WD_LAUNCHED(ctx);
-        return wd_red_finish(ctx, 0);
+        return wd_red_finish(ctx, slot);
     }
     wd_status accum(WdVec xs, WdVec xh) const
     {
@@ -289,6 +289,18 @@ wd_status wd_mx_from_h(wd_context *ctx, int Vh, wd_precision L, wd_precision H, 
 wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
                          const WdMxReliable &v, const WdVec *p_restart, double *rr, double *ss)
 {
+    wd_status e = wd_mx_reliable_enqueue(ctx, lat, mass, L, H, v, p_restart, 0);
+    if (e != WD_OK) return e;
+    double2 red[2];
+    if ((e = wd_red_fetch(ctx, 2, red)) != WD_OK) return e;
+    *rr = red[0].x;
+    *ss = red[1].x;
+    return WD_OK;
+}
+
+wd_status wd_mx_reliable_enqueue(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
+                                 const WdMxReliable &v, const WdVec *p_restart, int slot)
+{
     const int Vh = lat->g.Vh;
     const int64_t nh = (int64_t)12 * Vh;
     const Mixed mx{ctx, Vh, L, H};
@@ -302,12 +314,8 @@ wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd
     if ((e = wd_v_xpayz(ctx, v.bhat, make_double2(-1.0, 0.0), v.t_h, v.s_e, nh)) != WD_OK) return e;
     if ((e = mx.to_f32(v.s_e, s32)) != WD_OK) return e;
     if ((e = wd_apply_Mhat_v(ctx, lat, s32, v.rs, tmp32, mass, 1)) != WD_OK) return e;
-    if ((e = mx.norm2_f32(v.rs)) != WD_OK) return e;
-    if ((e = wd_v_norm2(ctx, v.s_e, nh, 1)) != WD_OK) return e;
-    double2 red[2];
-    if ((e = wd_red_fetch(ctx, 2, red)) != WD_OK) return e;
-    *rr = red[0].x;
-    *ss = red[1].x;
+    if ((e = mx.norm2_f32(v.rs, slot)) != WD_OK) return e;
+    if ((e = wd_v_norm2(ctx, v.s_e, nh, slot + 1)) != WD_OK) return e;
     return p_restart ? mx.f32_to(v.rs, *p_restart) : WD_OK;
 }
 

@@ -44,3 +44,7 @@ struct WdMxReliable {
 // ss = |s|^2; p_restart (storage L) <- rs when given
 wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
                          const WdMxReliable &v, const WdVec *p_restart, double *rr, double *ss);
+// the same with no host wait: |rs|^2 lands in reduction slot `slot`, |s|^2 in
+// slot + 1, for the caller to fetch (several systems per fetch)
+wd_status wd_mx_reliable_enqueue(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
+                                 const WdMxReliable &v, const WdVec *p_restart, int slot);
