@@ -1,7 +1,7 @@
 """The short entry-point names of the drop-in boundary (wd_ctx_create,
 wd_gauge_upload, wd_fermion_upload/download, wd_M, wd_cg), called through the
 C ABI: M against the oracle's DslashNew (relative L2 <= 1e-13) and wd_cg in
-its flag combinations judged by the FP64 true residual."""
+its flag combinations checked by the FP64 true residual."""
 import ctypes as C
 
 import numpy as np

@@ -1,5 +1,5 @@
 """CG on the GPU: the reference algorithm step for step against the oracle,
-and the even-odd solver judged by its FP64 true residual and its error
+and the even-odd solver checked by its FP64 true residual and its error
 against the oracle's solution."""
 import numpy as np
 import pytest

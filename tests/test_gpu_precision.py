@@ -3,7 +3,7 @@ them, against the FP64 oracle.
 
 Bars: double-float (df64) output within 1e-13 relative L2 of the oracle (the
 FP64 bar); FP32 with 12-real links within 2e-6; FP16 (per-site scale) within
-5e-3.  Every solve is judged by its FP64 true residual |b - Mx|/|b| <= 1e-10
+5e-3.  Every solve is checked by its FP64 true residual |b - Mx|/|b| <= 1e-10
 and its error against the oracle's 1e-13 solution <= 1e-9."""
 import numpy as np
 import pytest
@@ -77,7 +77,7 @@ def solve_case(wd, oracle, ctx):
     return dims, gauge, src, ctx.lattice(dims, gauge), sols
 
 
-def _judge(wd, oracle, dims, gauge, src, x, mass, xo, st):
+def _check_solution(wd, oracle, dims, gauge, src, x, mass, xo, st):
     assert st.converged, st.as_dict()
     assert st.true_residual <= 1e-10, st.as_dict()
     r = src - oracle.dslash_full(x, gauge, dims, mass, 0)
@@ -90,7 +90,7 @@ def test_cg_eo_df64(wd, oracle, solve_case, mass):
     dims, gauge, src, lat, sols = solve_case
     b, x = lat.field(src), lat.field()
     st = lat.solve(b, x, wd.solver_params(kind=wd.CG_EO, mass=mass, tol=1e-10, prec=wd.DF64))
-    _judge(wd, oracle, dims, gauge, src, x.download(), mass, sols[mass], st)
+    _check_solution(wd, oracle, dims, gauge, src, x.download(), mass, sols[mass], st)
 
 
 def test_cgnr_ref_df64_matches_fp64(wd, oracle, solve_case):
@@ -114,4 +114,4 @@ def test_mixed_cg(wd, oracle, solve_case, inner, reliable, mass):
     st = lat.solve(b, x, wd.solver_params(kind=wd.CG_EO, mass=mass, tol=1e-10, max_iter=4000, prec=inner,
                                           prec_reliable=reliable))
     assert st.reliable_updates >= 1
-    _judge(wd, oracle, dims, gauge, src, x.download(), mass, sols[mass], st)
+    _check_solution(wd, oracle, dims, gauge, src, x.download(), mass, sols[mass], st)
