@@ -4,6 +4,7 @@
 // container lives in, as in the reference.  Operators run on the GPU.
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <stdexcept>
 #include "lattice_fermion.h"
@@ -39,7 +40,7 @@ lattice_fermion::~lattice_fermion()
     A = nullptr;
 }
 
-void lattice_fermion::clean() { std::memset(A, 0, sizeof(std::complex<double>) * size); }
+void lattice_fermion::clean() { std::fill(A, A + size, std::complex<double>(0.0, 0.0)); }
 
 lattice_fermion &lattice_fermion::operator-(const lattice_fermion &a)
 {

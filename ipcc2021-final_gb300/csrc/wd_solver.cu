@@ -68,7 +68,7 @@ wd_status wd_true_residual(wd_context *ctx, const wd_lattice *lat, const double2
                            double mass, double *rel)
 {
     const int64_t n = lat->volume * 12;
-    WdVec vb{(void *)b}, vx{(void *)x}, vt{(void *)tmp};
+    WdVec vx{(void *)x}, vt{(void *)tmp};
     wd_status st = wd_apply_M_v(ctx, lat, vx, vt, mass, 0);
     if (st != WD_OK) return st;
     if ((st = wd_blas_xpayz(ctx, b, make_double2(-1.0, 0.0), tmp, tmp, n)) != WD_OK) return st;
@@ -76,7 +76,6 @@ wd_status wd_true_residual(wd_context *ctx, const wd_lattice *lat, const double2
     if ((st = wd_red_norm2(ctx, b, n, 1)) != WD_OK) return st;
     double2 r[2];
     if ((st = wd_red_fetch(ctx, 2, r)) != WD_OK) return st;
-    (void)vb;
     *rel = r[1].x > 0 ? std::sqrt(r[0].x / r[1].x) : std::sqrt(r[0].x);
     return WD_OK;
 }
