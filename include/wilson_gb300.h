@@ -273,6 +273,29 @@ int wd_tune_pin(int device, const char *kernel, int half_volume, int variant);
 /* Number of launch variants of a kernel, known after its first launch (else 0). */
 int wd_tune_variants(const char *kernel);
 
+/* ---- gauge-configuration files (host only) ------------------------------- */
+/* The reference's load_gauge reads one format (src/load_gauge.cpp:58-161);
+ * its refs/utils_nersc_lat.cpp reads NERSC and ILDG files.  All are read
+ * here into the reference layout (4 arrays of V*9 complex, eo order):
+ *   REF   big-endian doubles [site][mu][row][col][re,im], the payload the
+ *         whole file or ending 280 bytes before its end (LIME framing);
+ *   NERSC ASCII header, 3x3 or two-row (row 2 rebuilt) links, IEEE64/32,
+ *         big or little endian, DIMENSION_i checked against dims;
+ *   ILDG  the last V*72 big-endian values of the file (LIME binary record),
+ *         double precision when the file holds them, else single.
+ * AUTO takes NERSC when the file starts with BEGIN_HEADER, else REF when the
+ * size fits it, else single-precision ILDG.  format_found (optional)
+ * receives the format read.  BAD_DIMS when the file cannot hold the
+ * lattice, BAD_ARG when it cannot be opened or read. */
+typedef enum {
+    WD_GAUGE_FILE_AUTO = 0,
+    WD_GAUGE_FILE_REF = 1,
+    WD_GAUGE_FILE_NERSC = 2,
+    WD_GAUGE_FILE_ILDG = 3
+} wd_gauge_file_format;
+wd_status wd_read_gauge_file(const char *path, const int dims[4], int format, double *const gauge[4],
+                             int *format_found);
+
 /* ---- seeded synthetic inputs (host, deterministic) ---------------------- */
 /* Gauge links U = exp(i eps H) re-unitarised to SU(3), H Gaussian traceless
  * hermitian; written in the reference layout (4 arrays of V*9 complex). */

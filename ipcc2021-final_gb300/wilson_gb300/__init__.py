@@ -59,6 +59,7 @@ def _load() -> C.CDLL:
     d4 = C.POINTER(C.c_void_p)
     sigs = {
         "wd_context_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
+        "wd_read_gauge_file": (C.c_int, [C.c_char_p, ip, C.c_int, d4, ip]),
         "wd_ctx_create": (C.c_int, [C.c_int, C.POINTER(vp)]),
         "wd_ctx_destroy": (None, [vp]),
         "wd_gauge_upload": (C.c_int, [vp, d4, ip, C.POINTER(vp)]),
@@ -175,6 +176,21 @@ def tune_pin(kernel: str, half_volume: int, variant: int, device: int = 0) -> No
 def tune_variants(kernel: str) -> int:
     """Launch variants of a hopping kernel (0 until it has launched once)."""
     return lib.wd_tune_variants(kernel.encode())
+
+
+GAUGE_FILE_AUTO, GAUGE_FILE_REF, GAUGE_FILE_NERSC, GAUGE_FILE_ILDG = range(4)
+
+
+def read_gauge_file(path: str, dims, fmt: int = GAUGE_FILE_AUTO) -> tuple[list[np.ndarray], int]:
+    """A gauge-configuration file (reference / NERSC / ILDG) in the reference
+    layout (4 arrays of V*9); returns (links, format read)."""
+    V = volume(dims)
+    g = [np.empty(V * 9, np.complex128) for _ in range(4)]
+    found = C.c_int(-1)
+    st = lib.wd_read_gauge_file(str(path).encode(), _dims(dims), fmt, _gauge_ptrs(g), C.byref(found))
+    if st != OK:
+        raise WilsonError(st, f"cannot read gauge file {path}: {lib.wd_status_string(st).decode()}")
+    return g, found.value
 
 
 def gen_gauge(dims, seed: int, eps: float = 0.5) -> list[np.ndarray]:
