@@ -151,9 +151,13 @@ def cpu_baseline_port(gauge, src, dims, seconds: float = 12.0) -> dict:
         if time.perf_counter() - t0 > seconds or reps >= 50:
             break
     dt = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    orc.dslash_full(src, gauge, dims, MASS, 0)
+    full_ms = (time.perf_counter() - t0) * 1e3
     return {"value": BYTES_PER_SITE_F64 * vh / dt / 1e9, "unit": "GB/s", "cores": cores, "kind": "port",
             "sample": f"{reps} DslashoffdNew applications at {'x'.join(map(str, dims))} (full workload), "
-                      f"{dt * 1e3:.1f} ms each, C restatement with OpenMP over sites"}
+                      f"{dt * 1e3:.1f} ms each, C restatement with OpenMP over sites",
+            "dslash_new_ms": full_ms}
 
 
 def dslash_variants(wd, ctx, lat, src, stream, steps: int, vh: int, peak: float) -> dict:
@@ -594,6 +598,16 @@ def run_ours(args) -> None:
         }
         if args.prec == "f64":
             line["dslash_other_storage"] = dslash_variants(wd, ctx, lat, src, stream, min(args.steps, 300), vh, peak)
+            # the full operator (DslashNew: diagonal + both hopping halves), resident fields
+            n_full = max(3, min(args.steps, 100))
+            lat.dslash_full(fin, fout, MASS, 0)
+            ctx.sync()
+            e0.record(stream)
+            for _ in range(n_full):
+                lat.dslash_full(fin, fout, MASS, 0)
+            e1.record(stream)
+            e1.synchronize()
+            line["dslash_new_ms"] = e0.elapsed_time(e1) / n_full
         line["autotune"] = [{"kernel": k, "half_volume": v, "variant": var, "ms": ms}
                             for _, k, v, var, ms in wd.tune_report()]
         if not args.no_solver:

@@ -107,3 +107,32 @@ def test_driver_rejects_bad_arguments_before_touching_a_gpu():
     r = subprocess.run([str(exe), "0.1", "UNIT", "8", "8", "8", "8", "8", "8", "4", "8"], capture_output=True,
                        text=True)
     assert r.returncode == 1 and "subgrid == lattice" in r.stderr
+
+
+def test_tuner_pins_and_report(wd):
+    """Pinning a launch variant needs no GPU; the report lists it (ms -1)."""
+    wd.tune_pin("hop_f16", 12345, 1)
+    try:
+        rows = [r for r in wd.tune_report() if r[1] == "hop_f16" and r[2] == 12345]
+        assert rows == [(0, "hop_f16", 12345, 1, -1.0)]
+    finally:
+        wd.tune_pin("hop_f16", 12345, -1)
+    assert not [r for r in wd.tune_report() if r[2] == 12345]
+    with pytest.raises(ValueError):
+        wd.tune_pin("hop_f16", 0, 1)
+
+
+def test_tuner_cache_file_is_read(tmp_path):
+    """WD_TUNE_CACHE decisions are loaded before any timing (fresh process)."""
+    import os
+    import subprocess
+    import sys
+
+    cache = tmp_path / "tune.txt"
+    cache.write_text("0 hop_df64 4096 3 0.125000\n0 hop_f32 4096 2 0.010000\n")
+    code = ("import sys; sys.path.insert(0, %r); import wilson_gb300 as wd; "
+            "wd.tune_pin('hop_f64', 1, -1); print(sorted(wd.tune_report()))") % str(REPO / "ipcc2021-final_gb300")
+    env = dict(os.environ, WD_TUNE_CACHE=str(cache))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert "(0, 'hop_df64', 4096, 3, 0.125)" in out.stdout and "(0, 'hop_f32', 4096, 2, 0.01)" in out.stdout
