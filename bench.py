@@ -616,13 +616,16 @@ def run_ours(args) -> None:
                               **solver_bench(wd, ctx, lat, src, MASS, plans=args.solver_plans,
                                              profile=args.profile_solves)}
         if not args.no_solver_mixed:
-            sd = tuple(args.solver_dims)
-            slat = ctx.lattice(sd, wd.gen_gauge(sd, SEED, EPS))
-            line["solver_mixed"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, sd))}, "
-                                                f"mass {args.solver_mass}, seed 2",
-                                    **solver_bench(wd, ctx, slat, wd.gen_source(sd, SEED), args.solver_mass,
-                                                   plans=args.solver_plans, profile=args.profile_solves)}
-            slat.close()
+            # the mixed-precision configuration: mass 0.01 on 32^3x64 and on 48^3x96
+            for key, sd in (("solver_mixed", tuple(args.solver_dims)), ("solver_mixed_large", (48, 48, 48, 96))):
+                if key == "solver_mixed_large" and args.no_solver_large:
+                    continue
+                slat = ctx.lattice(sd, wd.gen_gauge(sd, SEED, EPS))
+                line[key] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, sd))}, "
+                                         f"mass {args.solver_mass}, seed 2",
+                             **solver_bench(wd, ctx, slat, wd.gen_source(sd, SEED), args.solver_mass,
+                                            plans=args.solver_plans, profile=args.profile_solves)}
+                slat.close()
         if not args.no_solver:
             line["small_config"] = small_config_bench(wd, ctx, not args.no_cpu_baseline)
         if not args.no_batch:
@@ -657,7 +660,8 @@ def main() -> None:
     ap.add_argument("--solver-dims", type=int, nargs=4, default=[32, 32, 32, 64],
                     help="lattice of the second solver measurement (mixed-precision configuration; 48 48 48 96 also)")
     ap.add_argument("--solver-mass", type=float, default=0.01)
-    ap.add_argument("--no-solver-mixed", action="store_true", help="skip the second solver measurement")
+    ap.add_argument("--no-solver-mixed", action="store_true", help="skip the mass-0.01 solver measurements")
+    ap.add_argument("--no-solver-large", action="store_true", help="skip the 48^3x96 solver measurement")
     ap.add_argument("--serve-requests", type=int, default=24,
                     help="requests per serving run (the configured workload has 2000; 0 skips serving)")
     ap.add_argument("--serve-requests-f64", type=int, default=None,
