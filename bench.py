@@ -557,9 +557,17 @@ def run_ours(args) -> None:
             ctx.check(wd.lib.wd_host_dslash_offd(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
                                                  wd._ptr(h_src), wd._ptr(h_dst), 0, 0))
         e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e, world)
+        # DslashNew (full M) through its host-buffer entry point, same buffers
+        ctx.check(wd.lib.wd_host_dslash_full(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
+                                             wd._ptr(h_src), wd._ptr(h_dst), MASS, 0))
+        t1 = time.perf_counter()
+        for _ in range(n_e2e):
+            ctx.check(wd.lib.wd_host_dslash_full(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
+                                                 wd._ptr(h_src), wd._ptr(h_dst), MASS, 0))
+        full_ms = (time.perf_counter() - t1) / n_e2e * 1e3
         e2e = {"value": replica_throughput(BYTES_PER_SITE_F64 * vh, e2e_s, world) / 1e9, "unit": "GB/s",
                "h2d_bytes_per_step": int(src.nbytes // 2), "d2h_bytes_per_step": int(src.nbytes // 2),
-               "steps": n_e2e, "ms_per_step": e2e_s * 1e3,
+               "steps": n_e2e, "ms_per_step": e2e_s * 1e3, "dslash_new_host_ms": full_ms,
                "path": "wd_host_dslash_offd (DslashoffdNew): the source parity it reads goes up and the "
                        "computed parity comes back in up to 16 time-slab chunks overlapped with compute on "
                        "two streams, the kernel working on the reference's site-major layout in the staging "

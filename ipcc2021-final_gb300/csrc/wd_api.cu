@@ -538,35 +538,31 @@ static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *
     return WD_OK;
 }
 
-// DslashoffdNew on host arrays, as a three-stage pipeline over time slabs:
-// uploads of the source (h2d stream), the hopping term of output chunks (two
-// compute streams) and downloads of finished output chunks (copy stream)
-// overlap.  Output chunk [t0, t1) reads source slices t0-1 .. t1 (the
+// Host-array operators as a three-stage pipeline over time slabs: uploads of
+// the source parities the operator reads (h2d stream), the arithmetic on
+// output chunks (two compute streams) and downloads of finished chunks (copy
+// stream) overlap.  Output chunk [t0, t1) reads source slices t0-1 .. t1 (the
 // hopping term reaches one slice in t), so it waits only for the upload
 // holding slice t1; uploads go in units of at most Lt/32 slices, enqueued
 // just ahead of the first chunk that needs them, so the first compute starts
 // after about a chunk and a unit have arrived.  Chunk 0 reads slice Lt-1 and
-// runs last.  Only the source parity the term reads (1-cb) is uploaded, and
-// the other parity of dest -- zero by the reference's semantics,
-// src/dslash_new.cpp:1398 -- is cleared on the host meanwhile.  The kernel
-// reads and writes the reference's site-major layout in the staging buffers,
-// so data goes from copy to arithmetic to copy with no layout conversion.
-extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
-                                         const double *src, double *dest, int dag, int cb)
+// runs last.  The kernels read and write the reference's site-major layout
+// in the staging buffers (source parities | output parities), so data goes
+// from copy to arithmetic to copy with no layout conversion.  `in_mask` and
+// `out_mask` select parity blocks (bit p = parity p); compute(stream, p, lo,
+// hi, in, out) enqueues output parity p's sites [lo, hi).
+template <class Compute>
+static wd_status host_pipeline(wd_context *ctx, const double *src, double *dest, int in_mask, int out_mask,
+                               Compute compute)
 {
-    wd_status st = host_prepare(ctx, dims, gauge);
-    if (st != WD_OK) return st;
-    if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
-    if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
     const wd_lattice *lat = ctx->host_lat;
     const WdGeom &g = lat->g;
     const int Vh = g.Vh, Lt = g.L[3];
     const int slab = g.Lxh * g.L[1] * g.L[2];  // sites of one parity per time slice
     const size_t half = (size_t)12 * Vh;       // complex entries of one parity
-    if ((st = ensure_staging(ctx, 2 * half * sizeof(double2))) != WD_OK) return st;
-    double2 *in_aos = (double2 *)ctx->staging, *out_aos = in_aos + half;
-    const double2 *src_half = (const double2 *)src + (1 - cb) * half;
-    double2 *dest_half = (double2 *)dest + cb * half;
+    wd_status st = ensure_staging(ctx, 4 * half * sizeof(double2));
+    if (st != WD_OK) return st;
+    double2 *in_aos = (double2 *)ctx->staging, *out_aos = in_aos + 2 * half;
     // compute chunks of at least 64k sites (at most WD_MAX_CHUNKS); upload units
     int n = std::min(std::min(WD_MAX_CHUNKS, Lt), Vh / 65536);
     if (n < 3) n = 1;
@@ -579,8 +575,11 @@ extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], con
         for (; uploaded <= unit; ++uploaded) {
             const size_t lo = (size_t)uploaded * us * slab * 12;
             const size_t hi = (size_t)std::min((uploaded + 1) * us, Lt) * slab * 12;
-            WD_CUDA(ctx, cudaMemcpyAsync(in_aos + lo, src_half + lo, (hi - lo) * sizeof(double2),
-                                         cudaMemcpyHostToDevice, ctx->h2d_stream));
+            for (int p = 0; p < 2; ++p)
+                if (in_mask & (1 << p))
+                    WD_CUDA(ctx, cudaMemcpyAsync(in_aos + p * half + lo, (const double2 *)src + p * half + lo,
+                                                 (hi - lo) * sizeof(double2), cudaMemcpyHostToDevice,
+                                                 ctx->h2d_stream));
             WD_CUDA(ctx, cudaEventRecord(ctx->chunk_in[uploaded], ctx->h2d_stream));
         }
         return WD_OK;
@@ -597,22 +596,30 @@ extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], con
         cudaStream_t cs = (i & 1) ? ctx->aux_stream : ctx->stream;
         WD_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->chunk_in[need], 0));
         const int lo = tb[j] * slab, hi = tb[j + 1] * slab;
-        if ((st = wd_hop_f64_aos_range(ctx, cs, lat, in_aos, out_aos, cb, dag, -0.5, lo, hi)) != WD_OK) return st;
+        for (int p = 0; p < 2; ++p)
+            if (out_mask & (1 << p))
+                if ((st = compute(cs, p, lo, hi, in_aos, out_aos)) != WD_OK) return st;
         WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[j], cs));
         WD_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[j], 0));
-        WD_CUDA(ctx, cudaMemcpyAsync(dest_half + (size_t)lo * 12, out_aos + (size_t)lo * 12,
-                                     (size_t)(hi - lo) * 12 * sizeof(double2), cudaMemcpyDeviceToHost,
-                                     ctx->copy_stream));
+        for (int p = 0; p < 2; ++p)
+            if (out_mask & (1 << p))
+                WD_CUDA(ctx, cudaMemcpyAsync((double2 *)dest + p * half + (size_t)lo * 12,
+                                             out_aos + p * half + (size_t)lo * 12,
+                                             (size_t)(hi - lo) * 12 * sizeof(double2), cudaMemcpyDeviceToHost,
+                                             ctx->copy_stream));
     }
-    // the untouched parity of dest is zero.  Four threads: the copies to and
-    // from host memory run meanwhile, and a wider team both competes with them
-    // for host memory bandwidth and, on a busy host, waits on descheduled
-    // threads (measured at 32^3x64: 2.03 ms per call with 2-8 threads, up to
-    // 4.4 ms with 16 on 16 cores).
-    double *zero = dest + (size_t)(1 - cb) * half * 2;
-    const int64_t nz = (int64_t)half * 2;
+    // a parity of dest the operator does not write is zero.  Four threads: the
+    // copies to and from host memory run meanwhile, and a wider team both
+    // competes with them for host memory bandwidth and, on a busy host, waits
+    // on descheduled threads (measured at 32^3x64: 2.03 ms per call with 2-8
+    // threads, up to 4.4 ms with 16 on 16 cores).
+    for (int p = 0; p < 2; ++p)
+        if (!(out_mask & (1 << p))) {
+            double *zero = dest + (size_t)p * half * 2;
+            const int64_t nz = (int64_t)half * 2;
 #pragma omp parallel for schedule(static) num_threads(4)
-    for (int64_t i = 0; i < nz; ++i) zero[i] = 0.0;
+            for (int64_t i = 0; i < nz; ++i) zero[i] = 0.0;
+        }
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->aux_stream));
@@ -620,16 +627,40 @@ extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], con
     return WD_OK;
 }
 
+// DslashoffdNew on host arrays: only the source parity the term reads (1-cb)
+// is uploaded, and the other parity of dest -- zero by the reference's
+// semantics, src/dslash_new.cpp:1398 -- is cleared on the host meanwhile.
+extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                                         const double *src, double *dest, int dag, int cb)
+{
+    wd_status st = host_prepare(ctx, dims, gauge);
+    if (st != WD_OK) return st;
+    if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
+    const size_t half = (size_t)12 * ctx->host_lat->g.Vh;
+    return host_pipeline(ctx, src, dest, 1 << (1 - cb), 1 << cb,
+                         [&](cudaStream_t cs, int p, int lo, int hi, const double2 *in, double2 *out) {
+                             return wd_hop_f64_aos_range(ctx, cs, ctx->host_lat, in + (1 - p) * half,
+                                                         out + p * half, nullptr, p, dag, -0.5, 0.0, lo, hi);
+                         });
+}
+
+// DslashNew / Dslash on host arrays (src/invert.cpp:123-156): both parities go
+// up and come back; each output parity p is (4+m) src_p - 1/2 D_{p,1-p} src_{1-p}
+// in one kernel per chunk.
 extern "C" wd_status wd_host_dslash_full(wd_context *ctx, const int dims[4], const double *const gauge[4],
                                          const double *src, double *dest, double mass, int dag)
 {
     wd_status st = host_prepare(ctx, dims, gauge);
     if (st != WD_OK) return st;
     if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
-    if ((st = wd_field_upload(ctx, ctx->host_f[0], src)) != WD_OK) return st;
-    if ((st = wd_dslash_full(ctx, ctx->host_lat, ctx->host_f[0], ctx->host_f[1], mass, dag, WD_PREC_F64)) != WD_OK)
-        return st;
-    return wd_field_download(ctx, ctx->host_f[1], dest);
+    const size_t half = (size_t)12 * ctx->host_lat->g.Vh;
+    const double a = 4.0 + mass;
+    return host_pipeline(ctx, src, dest, 3, 3,
+                         [&](cudaStream_t cs, int p, int lo, int hi, const double2 *in, double2 *out) {
+                             return wd_hop_f64_aos_range(ctx, cs, ctx->host_lat, in + (1 - p) * half,
+                                                         out + p * half, in + p * half, p, dag, -0.5, a, lo, hi);
+                         });
 }
 
 extern "C" wd_status wd_host_cg(wd_context *ctx, const int dims[4], const double *const gauge[4],

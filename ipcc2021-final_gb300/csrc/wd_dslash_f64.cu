@@ -109,15 +109,22 @@ struct HopF64AoS : HopF64<THREADS> {
     __device__ __forceinline__ void epilogue(int s, const double2 *acc) const
     {
         double2 *o = this->out + (size_t)s * 12;
+        if (this->x) {  // site-major x block of the output parity
+            const double2 *xv = this->x + (size_t)s * 12;
 #pragma unroll
-        for (int c = 0; c < 12; ++c) o[c] = this->scale.apply(acc[c]);
+            for (int c = 0; c < 12; ++c) o[c] = c_axpby(this->alpha, acc[c], this->beta, xv[c]);
+        } else {
+#pragma unroll
+            for (int c = 0; c < 12; ++c) o[c] = this->scale.apply(acc[c]);
+        }
     }
 };
 
 }  // namespace
 
 wd_status wd_hop_f64_aos_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_aos,
-                               double2 *out_aos, int cb, int dag, double alpha, int s_lo, int s_hi)
+                               double2 *out_aos, const double2 *x_aos, int cb, int dag, double alpha, double beta,
+                               int s_lo, int s_hi)
 {
     using P = HopF64AoS<64>;
     P p;
@@ -125,10 +132,10 @@ wd_status wd_hop_f64_aos_range(wd_context *ctx, cudaStream_t stream, const wd_la
     p.cb = cb;
     p.in = in_aos;
     p.gauge = lat->gauge;
-    p.x = nullptr;
+    p.x = x_aos;
     p.out = out_aos;
     p.alpha = alpha;
-    p.beta = 0.0;
+    p.beta = beta;
     p.scale = F64Scale::make(alpha);
     const int n = s_hi - s_lo;
     if (n <= 0) return WD_OK;

@@ -80,9 +80,11 @@ wd_status wd_hop_v(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, 
 // ---- pipelined host-buffer path: one parity block, output sites [s_lo, s_hi), given stream
 wd_status wd_hop_f64_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_block,
                            double2 *out_block, int cb, int dag, double alpha, int s_lo, int s_hi);
-// the same on AoS (reference-layout) input and output parity blocks
+// the same on AoS (reference-layout) input and output parity blocks; with
+// x_aos (the output parity's AoS block) out = alpha * hop + beta * x
 wd_status wd_hop_f64_aos_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_aos,
-                               double2 *out_aos, int cb, int dag, double alpha, int s_lo, int s_hi);
+                               double2 *out_aos, const double2 *x_aos, int cb, int dag, double alpha, double beta,
+                               int s_lo, int s_hi);
 // aos holds sites [s_lo, s_hi) of one parity block, 12 complex per site; soa_block is the block's planes
 wd_status wd_range_aos_to_soa(wd_context *ctx, cudaStream_t stream, int Vh, const double2 *aos, double2 *soa_block,
                               int s_lo, int s_hi);

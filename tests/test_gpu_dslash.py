@@ -119,3 +119,15 @@ def test_volume_beyond_32bit_byte_offsets(wd, ctx, oracle):
         fi.close()
         fo.close()
     lat.close()
+
+
+@pytest.mark.parametrize("dims,dag", [((16, 16, 16, 16), 0), ((24, 24, 24, 32), 1), ((32, 32, 32, 64), 0)])
+def test_host_full_pipelined(wd, ctx, oracle, dims, dag):
+    """The host-buffer DslashNew (both parities up and back) in one piece and
+    as overlapped time-slab chunks, against the oracle."""
+    gauge = wd.gen_gauge(dims, seed=6)
+    src = wd.gen_source(dims, seed=6)
+    out = np.full_like(src, np.nan + 1j)
+    from wilson_gb300 import _dims, _gauge_ptrs, _ptr, lib
+    ctx.check(lib.wd_host_dslash_full(ctx.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(src), _ptr(out), 0.07, dag))
+    assert rel_l2(out, oracle.dslash_full(src, gauge, dims, 0.07, dag)) < TOL
