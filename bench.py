@@ -11,8 +11,16 @@ per spinor parity) are larger than L2 (129 MB), so no flush is needed.
 
 `e2e` measures the same metric through the reference-facing host-buffer
 entry point (wd_host_dslash_offd = DslashoffdNew): every step copies the
-reference-layout source from pinned host memory to the device, converts the
-layout, applies the hopping term, and copies the full destination back.
+source parity the term reads from pinned host memory to the device, applies
+the hopping term on the reference's site-major layout, and returns the
+computed parity (the other parity of the destination is zeroed on the host),
+in overlapped time-slab chunks.
+
+Beside the headline line: the other storage formats (double-float, FP32,
+FP16), DslashNew, CG solves per arithmetic at 32^3x64 (mass 0.05 and 0.01)
+and 48^3x96 (mass 0.01), the reference's own 8^3x16 case, batched solves
+(24 right-hand sides; 16 lattices of uneven volume), a continuous-batching
+serving run, and the CPU baseline.
 
 Multi-GPU: replicas only (the reference's domain decomposition is replaced by
 one lattice per GPU); value = sum over ranks of per-rank work / max time.
