@@ -3,7 +3,7 @@
 // Same algorithm and memory traffic as the FP64 kernel (1536 B per output
 // site: every complex number is a 16-byte float4 {re.h, im.h, re.l, im.l}),
 // with the arithmetic moved from the FP64 pipe to the FP32 pipe
-// (wd_df.cuh): ~8.5k FP32 operations per site instead of ~890 FP64 ones.
+// (wd_df.cuh): ~8.5k FP32 operations per site instead of ~790 FP64 ones.
 // Results agree with FP64 to ~1e-14 relative L2 (storage rounding 2^-49,
 // arithmetic ~2^-48 per operation).
 //

@@ -4,7 +4,10 @@
 // Algorithmic traffic per output site: 8 links x 144 B + 1 spinor in x 192 B
 // + 1 spinor out x 192 B = 1536 B (+192 B when the epilogue reads x).
 // Arithmetic: 1320 flop per site.  On GB300 the FP64 pipe (~1.2 TFLOP/s
-// measured) rather than HBM bounds this kernel; wd_dslash_df.cu holds the
+// measured) rather than HBM bounds this kernel, so it is written for the
+// fewest FP64 operations (~790 per site): direction pairs combined
+// (wd_hop_mu), the first direction assigned, and a power-of-two output scale
+// applied on the exponent bits (F64Scale).  wd_dslash_df.cu holds the
 // double-float variant that moves the arithmetic onto the FP32 pipe.
 #include <cmath>
 #include <cstdint>

@@ -4,8 +4,9 @@
 //
 // Compulsory bytes per output site: FP32 8*48 + 96 + 96 = 576 B;
 // FP16 8*24 + 52 + 52 = 296 B (+ one spinor read when the epilogue uses x).
-// Both are HBM-bound: 1320 flop/site (+ 8 x 66 for the row-2 rebuild) is far
-// below the FP32 ridge.
+// 1320 flop/site (+ 8 x 66 for the row-2 rebuild) is far below the FP32
+// ridge: FP32 runs at the HBM bound, FP16 (half the bytes, the same
+// arithmetic plus unpacking) at the instruction-issue bound.
 #include "wd_hop.cuh"
 #include "wd_lp.cuh"
 #include "wd_kernels.h"

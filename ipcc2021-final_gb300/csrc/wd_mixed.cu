@@ -7,9 +7,9 @@
 // per-site double-float partial sums reduced in FP64.  Whenever the
 // low-precision residual has dropped by delta (default 0.1) since the last
 // update, or has reached the estimated target, a reliable update
-// (Sleijpen & van der Vorst) runs in high precision (FP64, or double-float
-// when prec_reliable = WD_PREC_DF64):
-//   x_e += x_s;  s = bhat - Mhat x_e;  r = Mhat^dag s;  r_s <- r;  x_s <- 0
+// (Sleijpen & van der Vorst) recomputes the residual in high precision (FP64,
+// or double-float when prec_reliable = WD_PREC_DF64):
+//   x_e += x_s;  s = bhat - Mhat x_e;  r_s = Mhat^dag s (FP32);  x_s <- 0
 // |s| is the true residual |b - M x| of the full system, so convergence is
 // decided on the recomputed high-precision residual, never on the iterated one.
 #include <chrono>
