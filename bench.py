@@ -252,8 +252,9 @@ SOLVER_PLANS = ("f64", "df64", "mixed_f32", "mixed_f16", "mixed_f16_df64")
 
 def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10, plans=SOLVER_PLANS,
                  profile: bool = False) -> dict:
-    """One solve per arithmetic on the resident lattice: solves/s, iterations,
-    FP64 true residual, and the relative difference to the FP64 solution.
+    """Solves per arithmetic on the resident lattice (the median of three timed
+    solves after a warm-up): solves/s, iterations, FP64 true residual, and the
+    relative difference to the FP64 solution.
     profile=True brackets each timed solve with cudaProfilerStart/Stop (for
     `ncu --profile-from-start off`)."""
     import torch
@@ -268,17 +269,21 @@ def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10, plans=SOLVE
         x = lat.field()
         p = wd.solver_params(kind=wd.CG_EO, mass=mass, tol=tol, max_iter=5000, prec=prec, prec_reliable=rel)
         lat.solve(b, x, p)            # warm-up (derived link copies, allocator)
-        x.zero()
-        ctx.sync()
-        if profile:
-            torch.cuda.profiler.start()
-        st = lat.solve(b, x, p)
-        if profile:
-            torch.cuda.profiler.stop()
+        times = []
+        for rep in range(1 if profile else 3):  # the median of three timed solves
+            x.zero()
+            ctx.sync()
+            if profile:
+                torch.cuda.profiler.start()
+            st = lat.solve(b, x, p)
+            if profile:
+                torch.cuda.profiler.stop()
+            times.append(st.seconds)
+        secs = float(np.median(times))
         sol = x.download()
         if ref is None:
             ref = sol
-        out[name] = {"solves_per_s": 1.0 / st.seconds, "seconds": st.seconds, "iterations": st.iterations,
+        out[name] = {"solves_per_s": 1.0 / secs, "seconds": secs, "seconds_each": times, "iterations": st.iterations,
                      "reliable_updates": st.reliable_updates, "true_residual": st.true_residual,
                      "rel_diff_vs_f64": float(np.linalg.norm(sol - ref) / np.linalg.norm(ref))}
         x.close()
