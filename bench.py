@@ -496,9 +496,11 @@ def run_reference(args) -> None:
     v = BYTES_PER_SITE_F64 * vh / dt / 1e9
     line = {"metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": world, "steps": n, "warmup": args.warmup,
             "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded SU(3) links eps=0.5, Gaussian source)",
-            "config": {"workload": "D_eo FP64 32^3x64, seed 2", "lattice": list(DIMS), "sites": int(np.prod(DIMS)),
-                       "parallelism": "host threads"},
+            "dtype": "f64", "data": "synthetic (seeded SU(3) links eps=0.5, unit Gaussian source)",
+            "config": {"workload": f"even-odd Dslash D_eo, {'x'.join(map(str, DIMS))}, seed 2 "
+                                   f"({n} repeated applications)",
+                       "lattice": list(DIMS), "sites": int(np.prod(DIMS)), "precision": "f64",
+                       "parallelism": f"host threads x{cores}"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "GB/s", "cores": cores, "kind": "port",
                              "sample": f"{n} DslashoffdNew applications at 32x32x32x64 (C restatement of the "
