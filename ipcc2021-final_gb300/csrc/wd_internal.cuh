@@ -35,6 +35,7 @@ struct wd_context {
     cudaStream_t copy_stream = nullptr;  // device->host copies overlapped with compute
     cudaStream_t h2d_stream = nullptr;   // host->device copies overlapped with compute
     cudaStream_t aux_stream = nullptr;   // second compute stream of the pipelined host path
+    int pageable_access = 0;             // the device reads and writes pageable host memory
     cudaEvent_t chunk_done[WD_MAX_CHUNKS] = {};  // compute -> copy hand-off of the pipelined host path
     cudaEvent_t chunk_in[WD_MAX_UPLOADS] = {};   // upload -> compute hand-off
     std::string last_error;

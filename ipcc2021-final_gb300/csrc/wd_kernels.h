@@ -80,6 +80,9 @@ wd_status wd_hop_v(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, 
 // ---- pipelined host-buffer path: one parity block, output sites [s_lo, s_hi), given stream
 wd_status wd_hop_f64_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_block,
                            double2 *out_block, int cb, int dag, double alpha, int s_lo, int s_hi);
+// n 16-byte entries src -> dst by a kernel on `stream` (for host memory the
+// device addresses directly)
+wd_status wd_copy_kernel(wd_context *ctx, cudaStream_t stream, const double2 *src, double2 *dst, int64_t n);
 // the same on AoS (reference-layout) input and output parity blocks; with
 // x_aos (the output parity's AoS block) out = alpha * hop + beta * x
 wd_status wd_hop_f64_aos_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_aos,

@@ -131,3 +131,24 @@ def test_host_full_pipelined(wd, ctx, oracle, dims, dag):
     from wilson_gb300 import _dims, _gauge_ptrs, _ptr, lib
     ctx.check(lib.wd_host_dslash_full(ctx.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(src), _ptr(out), 0.07, dag))
     assert rel_l2(out, oracle.dslash_full(src, gauge, dims, 0.07, dag)) < TOL
+
+
+def test_host_paths_pinned_and_pageable_buffers(wd, ctx, oracle):
+    """Pinned host buffers go through the copy engines, pageable ones
+    through kernels that address host memory directly: both give the
+    oracle's result (DslashoffdNew and DslashNew, 24^3x32, chunked)."""
+    torch = pytest.importorskip("torch")
+    dims = (24, 24, 24, 32)
+    gauge = wd.gen_gauge(dims, seed=8)
+    src = wd.gen_source(dims, seed=8)
+    from wilson_gb300 import _dims, _gauge_ptrs, _ptr, lib
+    want_offd = oracle.dslash_offd(src, gauge, dims, 1, 0)
+    want_full = oracle.dslash_full(src, gauge, dims, 0.2, 0)
+    pinned_src = torch.from_numpy(src).pin_memory().numpy()
+    pinned_out = torch.empty(src.size, dtype=torch.complex128).pin_memory().numpy()
+    for s, o in ((pinned_src, pinned_out), (src.copy(), np.empty_like(src))):
+        o[:] = np.nan
+        ctx.check(lib.wd_host_dslash_offd(ctx.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(s), _ptr(o), 1, 0))
+        assert rel_l2(o, want_offd) < TOL
+        ctx.check(lib.wd_host_dslash_full(ctx.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(s), _ptr(o), 0.2, 0))
+        assert rel_l2(o, want_full) < TOL
