@@ -51,3 +51,27 @@ def ctx(wd):
     c = wd.Context(0)
     yield c
     c.close()
+
+
+@pytest.fixture(scope="session")
+def digest8(wd):
+    """The 8^3x16 fixture: digests of the reference's outputs plus its seeded
+    inputs regenerated with the package's host generator."""
+    z = np.load(GOLDEN / "wilson_8x8x8x16_digest.npz")
+    d = {k: z[k] for k in z.files}
+    dims = tuple(int(v) for v in d["dims"])
+    d["dims"] = dims
+    d["mass"] = float(d["mass"])
+    d["stride"] = int(d["stride"])
+    d["gauge"] = wd.gen_gauge(dims, seed=int(d["gauge_seed"]), eps=float(d["eps"]))
+    d["src"] = wd.gen_source(dims, seed=int(d["source_seed"]))
+    return d
+
+
+def digest_error(d, name, v) -> float:
+    """Largest of the relative errors of v's L2 norm and of its sampled
+    entries against the fixture's digest of `name`."""
+    ref = d[f"{name}_sample"]
+    e_sample = np.linalg.norm(v[::d["stride"]] - ref) / np.linalg.norm(ref)
+    e_norm = abs(np.linalg.norm(v) - float(d[f"{name}_norm"])) / float(d[f"{name}_norm"])
+    return float(max(e_sample, e_norm))

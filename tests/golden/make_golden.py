@@ -6,8 +6,14 @@ compiled single-rank against oracle/mpi_shim/mpi.h (oracle/_ref/libref.so,
 built by `make -C oracle`).  Inputs are generated here with numpy (seeded), so
 the fixtures are self-contained: every array the check needs is stored.
 
+The third fixture covers the 8^3x16 configuration (V = 8192, seed 1, mass 0.1,
+links exp(i 0.5 H) and a unit Gaussian source from the package's own seeded
+host generator, wd_gen_gauge / wd_gen_source).  Its vectors are too large to
+store whole, so it keeps digests of the reference's outputs: the L2 norm of
+each and its entries at every 37th index.
+
 Run from the repository root, on an x86-64 host with the reference tree:
-    make -C oracle && python tests/golden/make_golden.py
+    python -c "import __graft_entry__ as g; g.build()" && python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -19,7 +25,10 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent / "oracle"))
+sys.path.insert(0, str(HERE.parent.parent / "ipcc2021-final_gb300"))
 from oracle import Reference  # noqa: E402
+
+DIGEST_STRIDE = 37  # sampled entries of each stored 8^3x16 vector
 
 
 def su3_links(rng: np.random.Generator, n: int, eps: float) -> np.ndarray:
@@ -89,6 +98,28 @@ def main() -> None:
     out["offd_new_dag0_cb1"] = ref.dslashoffd_new(src, gauge, dims, 0, 1)
     np.savez_compressed(HERE / "wilson_6x4x2x4.npz", **out)
     print("golden vectors written; CG:", iters, "iterations, |r| =", rsd)
+
+    # 3) 8^3x16 with the package's generator: digests of every entry point and of CGinvert
+    import wilson_gb300 as wd
+    dims, mass = (8, 8, 8, 16), 0.1
+    gauge, src = wd.gen_gauge(dims, seed=1, eps=0.5), wd.gen_source(dims, seed=1)
+    out = {"dims": np.array(dims), "mass": mass, "gauge_seed": 1, "source_seed": 1, "eps": 0.5,
+           "stride": DIGEST_STRIDE}
+
+    def digest(name, v):
+        out[f"{name}_norm"] = np.linalg.norm(v)
+        out[f"{name}_sample"] = np.ascontiguousarray(v[::DIGEST_STRIDE])
+
+    for dag in (0, 1):
+        for cb in (0, 1):
+            digest(f"offd_new_dag{dag}_cb{cb}", ref.dslashoffd_new(src, gauge, dims, dag, cb))
+        digest(f"full_new_dag{dag}", ref.dslash_new(src, gauge, dims, mass, dag))
+    digest("full_old_dag1", ref.dslash_old(src, gauge, dims, mass, 1))
+    x, iters, rsd = ref.cginvert(src, gauge, dims, mass, 1000, 1e-10, 7)
+    out.update(cg_seed=7, cg_max=1000, cg_acc=1e-10, cg_iters=iters, cg_rsd=rsd)
+    digest("cg_x", x)
+    np.savez_compressed(HERE / "wilson_8x8x8x16_digest.npz", **out)
+    print("8^3x16 digests written; CG:", iters, "iterations, |r| =", rsd)
 
 
 if __name__ == "__main__":

@@ -73,3 +73,16 @@ def test_not_converged_is_reported(wd, ctx):
         ctx.host_cg(dims, gauge, src, np.zeros_like(src),
                     wd.solver_params(kind=wd.CG_EO, mass=0.1, tol=1e-12, max_iter=3))
     assert e.value.status == wd.NOT_CONVERGED
+
+
+def test_cgnr_ref_matches_reference_digest_8c16(wd, ctx, oracle, digest8):
+    """CGinvert at 8^3x16 (m = 0.1, srand(7) initial guess, 1e-10) against the
+    reference's own iteration count, residual and solution digest."""
+    from conftest import digest_error
+    d = digest8
+    x = oracle.rand_guess(d["src"].size, int(d["cg_seed"]))
+    p = wd.solver_params(kind=wd.CGNR_REF, mass=d["mass"], tol=float(d["cg_acc"]), max_iter=int(d["cg_max"]))
+    st = ctx.host_cg(d["dims"], d["gauge"], d["src"], x, p)
+    assert abs(st.iterations - int(d["cg_iters"])) <= 1
+    assert abs(st.residual - float(d["cg_rsd"])) < 0.05 * float(d["cg_rsd"])
+    assert digest_error(d, "cg_x", x) < 1e-9

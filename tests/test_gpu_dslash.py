@@ -152,3 +152,23 @@ def test_host_paths_pinned_and_pageable_buffers(wd, ctx, oracle):
         assert rel_l2(o, want_offd) < TOL
         ctx.check(lib.wd_host_dslash_full(ctx.handle, _dims(dims), _gauge_ptrs(gauge), _ptr(s), _ptr(o), 0.2, 0))
         assert rel_l2(o, want_full) < TOL
+
+
+def test_reference_digests_8c16(wd, ctx, digest8):
+    """8^3x16, m = 0.1, seed 1 against the reference's own outputs (digests):
+    host-buffer entry points and the resident lattice."""
+    from conftest import digest_error
+    d = digest8
+    g, src, dims, m = d["gauge"], d["src"], d["dims"], d["mass"]
+    lat = ctx.lattice(dims, g)
+    fs, fo = lat.field(src), lat.field()
+    for dag in (0, 1):
+        for cb in (0, 1):
+            name = f"offd_new_dag{dag}_cb{cb}"
+            assert digest_error(d, name, ctx.host_dslash_offd(dims, g, src, dag, cb)) < TOL, name
+            lat.dslash_offd(fs, fo, dag, cb)
+            assert digest_error(d, name, fo.download()) < TOL, name
+        name = f"full_new_dag{dag}"
+        assert digest_error(d, name, ctx.host_dslash_full(dims, g, src, m, dag)) < TOL, name
+        lat.dslash_full(fs, fo, m, dag)
+        assert digest_error(d, name, fo.download()) < TOL, name

@@ -125,3 +125,21 @@ def test_gauge_covariance(oracle, golden6):
     outn = oracle.dslash_full(np.ascontiguousarray(psin), [np.ascontiguousarray(u.reshape(-1)) for u in Un],
                               dims, 0.05, 0)
     assert rel_l2(outn, np.einsum("sab,sib->sia", W, out).reshape(-1)) < 1e-13
+
+
+def test_oracle_matches_reference_digests_8c16(oracle, digest8):
+    """8^3x16, m = 0.1, seed 1: every entry point and CGinvert (srand(7)
+    initial guess, 1e-10, 1000 iterations) against the reference's digests."""
+    from conftest import digest_error
+    d = digest8
+    g, src, dims, m = d["gauge"], d["src"], d["dims"], d["mass"]
+    for dag in (0, 1):
+        for cb in (0, 1):
+            assert digest_error(d, f"offd_new_dag{dag}_cb{cb}", oracle.dslash_offd(src, g, dims, dag, cb)) < 1e-14
+        assert digest_error(d, f"full_new_dag{dag}", oracle.dslash_full(src, g, dims, m, dag)) < 1e-14
+    assert digest_error(d, "full_old_dag1", oracle.dslash_full(src, g, dims, m, 1)) < 1e-14
+    x0 = oracle.rand_guess(src.size, int(d["cg_seed"]))
+    x, iters, rsd = oracle.cg_ref(src, g, dims, m, int(d["cg_max"]), float(d["cg_acc"]), x0)
+    assert iters == int(d["cg_iters"])
+    assert abs(rsd - float(d["cg_rsd"])) < 1e-6 * float(d["cg_rsd"])
+    assert digest_error(d, "cg_x", x) < 1e-11
