@@ -465,7 +465,9 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
     // prefetch of the next direction [0.153 ms, 100.9 M, stalls 3.5].  Every
     // form tried lands at ~55 % of the FMA pipe.  Dropped: the unbounded
     // colour-split form (242 registers, 0.225 ms), the register-prefetching
-    // packed form (0.180 ms), L2 prefetch on the scalar form (0.161 ms).
+    // packed form (0.180 ms), L2 prefetch on the scalar form (0.161 ms), the
+    // pipelined form capped at 80 or 72 registers (550-830 bytes of spills;
+    // 0.205 and 0.244 ms).
     using F = std::false_type;
     using T = std::true_type;
     using W2 = std::integral_constant<int, 2>;

@@ -15,10 +15,12 @@
 
 namespace {
 
-template <class Sp, class Lk, int THREADS = 128>
+// THREADS per block; MINB blocks per SM as an occupancy hint (0: none)
+template <class Sp, class Lk, int THREADS = 128, int MINB = 0>
 struct HopLP {
     using C = float2;
     static constexpr int kThreads = THREADS;
+    static constexpr int kMinBlocks = MINB;
     static constexpr bool kSiteScale = Sp::kScaled;
     WdGeom g;
     int cb;
@@ -155,20 +157,29 @@ wd_status launch_hop(wd_context *ctx, const P &p, int dag)
     return WD_OK;
 }
 
-// the same operands launched with 128, 64 or 256 threads per block (tuned)
+// the same operands in the launch variants the tuner times: 128, 64 or 256
+// threads per block, or 128 with registers capped for 8 blocks per SM
+// (GB300, FP16 D_eo at 32^3x64: 75.8, 75.8, 81.9, 74.2 us; FP32 all within
+// 1 % of 102.5 us).  A software-pipelined form issuing the next direction's
+// loads before the current direction's arithmetic ran no faster (76.1 and
+// 102.4 us): the compiler already hoists those loads.
 template <class Sp, class Lk>
 wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p, int dag)
 {
-    return wd_tune_launch(ctx, name, p.g.Vh, 3, [&](int v) -> wd_status {
-        auto with = [&](auto tag) {
-            HopLP<Sp, Lk, decltype(tag)::value> q;
+    return wd_tune_launch(ctx, name, p.g.Vh, 4, [&](int v) -> wd_status {
+        auto with = [&](auto threads, auto minb) {
+            HopLP<Sp, Lk, decltype(threads)::value, decltype(minb)::value> q;
             q.g = p.g, q.cb = p.cb, q.in = p.in, q.out = p.out, q.x = p.x, q.link = p.link;
             q.has_x = p.has_x, q.alpha = p.alpha, q.beta = p.beta;
             return launch_hop(ctx, q, dag);
         };
-        if (v == 1) return with(std::integral_constant<int, 64>());
-        if (v == 2) return with(std::integral_constant<int, 256>());
-        return with(std::integral_constant<int, 128>());
+        using I0 = std::integral_constant<int, 0>;
+        switch (v) {
+        case 1: return with(std::integral_constant<int, 64>(), I0());
+        case 2: return with(std::integral_constant<int, 256>(), I0());
+        case 3: return with(std::integral_constant<int, 128>(), std::integral_constant<int, 8>());
+        default: return with(std::integral_constant<int, 128>(), I0());
+        }
     });
 }
 

@@ -307,8 +307,15 @@ __device__ __forceinline__ void wd_hop_site(const P &p, int s, typename P::C *ac
     }
 }
 
+// Optional occupancy hint: `static constexpr int kMinBlocks` (blocks per SM
+// the register allocation must allow; 0 = no hint).
+template <class P, class = void>
+struct wd_min_blocks : std::integral_constant<int, 0> {};
+template <class P>
+struct wd_min_blocks<P, std::void_t<decltype(P::kMinBlocks)>> : std::integral_constant<int, P::kMinBlocks> {};
+
 template <bool DAG, class P>
-__global__ void __launch_bounds__(P::kThreads) wd_hop_kernel(const P p)
+__global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) wd_hop_kernel(const P p)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.g.Vh) return;
@@ -319,7 +326,8 @@ __global__ void __launch_bounds__(P::kThreads) wd_hop_kernel(const P p)
 
 // The same over output sites [s_lo, s_hi) only (pipelined host-buffer path).
 template <bool DAG, class P>
-__global__ void __launch_bounds__(P::kThreads) wd_hop_kernel_range(const P p, int s_lo, int s_hi)
+__global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) wd_hop_kernel_range(const P p, int s_lo,
+                                                                                               int s_hi)
 {
     const int s = s_lo + blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= s_hi) return;

@@ -12,6 +12,7 @@
 #pragma once
 #include <cuda_fp16.h>
 #include "wd_internal.cuh"
+#include "wd_complex.cuh"
 
 __device__ __forceinline__ float2 h2f(__half2 h) { return __half22float2(h); }
 __device__ __forceinline__ __half2 f2h(float2 f) { return __float22half2_rn(f); }
@@ -95,13 +96,14 @@ inline SpF16 sp_f16(WdVec v, int Vh) { return SpF16{(uint4 *)v.p, v.scale, Vh}; 
 // ------------------------------------------------------------ links (12-real)
 __device__ __forceinline__ void su3_row2(float2 *U)
 {
-    // U[6..8] = conj(row0 x row1)
+    // U[6..8] = conj(row0 x row1), with explicit FMAs (c_mul) so every kernel
+    // that rebuilds a link rounds it identically
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         const int a = (k + 1) % 3, b = (k + 2) % 3;
-        const float2 p = make_float2(U[a].x * U[3 + b].x - U[a].y * U[3 + b].y, U[a].x * U[3 + b].y + U[a].y * U[3 + b].x);
-        const float2 q = make_float2(U[b].x * U[3 + a].x - U[b].y * U[3 + a].y, U[b].x * U[3 + a].y + U[b].y * U[3 + a].x);
-        U[6 + k] = make_float2(p.x - q.x, -(p.y - q.y));
+        const float2 p = c_mul(U[a], U[3 + b]);
+        const float2 q = c_mul(U[b], U[3 + a]);
+        U[6 + k] = make_float2(p.x - q.x, q.y - p.y);
     }
 }
 
