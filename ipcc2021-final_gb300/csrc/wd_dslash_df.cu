@@ -14,6 +14,14 @@
 // Loads stay non-redundant, registers fall from ~144 to ~90 per thread and
 // three times as many threads are in flight to hide memory latency.  A warp
 // holds 10 sites (lanes 0-9 colour 0, 10-19 colour 1, 20-29 colour 2).
+//
+// Two kernels on that mapping, bit-identical to each other:
+//   k_hop_df_staged  each thread copies the next direction's seven operands
+//                    into shared memory with cp.async while it computes the
+//                    current one with the packed (re, im) arithmetic of
+//                    wd_df2.cuh (half the instructions); the default;
+//   k_hop_df_pipe    scalar arithmetic, the next direction's operands loaded
+//                    into registers ahead of use.
 #include "wd_hop.cuh"
 #include "wd_df.cuh"
 #include "wd_df2.cuh"
@@ -45,45 +53,6 @@ __device__ __forceinline__ dfc shfl_dfc(const dfc &v, int src)
 __device__ __forceinline__ dfc ld(const float4 *p, size_t i, bool on)
 {
     return on ? df_from_f4(p[i]) : c_zero(dfc());
-}
-
-template <int MU, bool FWD, bool DAG>
-__device__ __forceinline__ void split_dir(const SplitDF &p, int s, const WdSite &cs, int col, int c1, int c2,
-                                          int src1, int src2, bool on, dfc *acc)
-{
-    constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
-    const size_t Vh = p.g.Vh;
-    const int nb = wd_neighbour(p.g, s, cs, MU, FWD);
-    dfc h0, h1;
-    {
-        const dfc s0 = ld(p.in, (0 + col) * Vh + nb, on), s1 = ld(p.in, (3 + col) * Vh + nb, on);
-        const dfc s2 = ld(p.in, (6 + col) * Vh + nb, on), s3 = ld(p.in, (9 + col) * Vh + nb, on);
-        wd_proj1<MU, SG>(s0, s1, s2, s3, h0, h1);
-    }
-    // W[col][b] for b = col, c1, c2: forward row col of U_mu(x); backward
-    // conj of column col of U_mu(x - mu)
-    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? s : nb);
-    dfc wa, wb, wc;
-    if constexpr (FWD) {
-        wa = ld(gb, (size_t)(col * 3 + col) * Vh, on);
-        wb = ld(gb, (size_t)(col * 3 + c1) * Vh, on);
-        wc = ld(gb, (size_t)(col * 3 + c2) * Vh, on);
-    } else {
-        wa = ld(gb, (size_t)(col * 3 + col) * Vh, on);
-        wb = ld(gb, (size_t)(c1 * 3 + col) * Vh, on);
-        wc = ld(gb, (size_t)(c2 * 3 + col) * Vh, on);
-    }
-    const dfc h0b = shfl_dfc(h0, src1), h1b = shfl_dfc(h1, src1);
-    const dfc h0c = shfl_dfc(h0, src2), h1c = shfl_dfc(h1, src2);
-    dfc t0, t1;
-    if constexpr (FWD) {
-        t0 = c_madd(c_madd(c_mul(wa, h0), wb, h0b), wc, h0c);
-        t1 = c_madd(c_madd(c_mul(wa, h1), wb, h1b), wc, h1c);
-    } else {
-        t0 = c_maddc(c_maddc(c_mulc(wa, h0), wb, h0b), wc, h0c);
-        t1 = c_maddc(c_maddc(c_mulc(wa, h1), wb, h1b), wc, h1c);
-    }
-    wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
 }
 
 // Software-pipelined form: the loads of the next direction are issued
@@ -138,33 +107,9 @@ __device__ __forceinline__ void split_compute(const SplitCtx &x, const DirLoad &
     wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
 }
 
-// L2 prefetch of one direction's operands (the addresses split_load reads):
-// no registers held, so the next direction's requests are in flight while
-// the current one computes.
-__device__ __forceinline__ void pf_l2(const float4 *a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); }
-
-template <int MU, bool FWD>
-__device__ __forceinline__ void split_prefetch(const SplitDF &p, const SplitCtx &x)
-{
-    if (!x.on) return;
-    const size_t Vh = p.g.Vh;
-    const int nb = wd_neighbour(p.g, x.s, x.cs, MU, FWD);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) pf_l2(p.in + (size_t)(k * 3 + x.col) * Vh + nb);
-    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? x.s : nb);
-    if constexpr (FWD) {
-        pf_l2(gb + (size_t)(x.col * 3 + x.col) * Vh);
-        pf_l2(gb + (size_t)(x.col * 3 + x.c1) * Vh);
-        pf_l2(gb + (size_t)(x.col * 3 + x.c2) * Vh);
-    } else {
-        pf_l2(gb + (size_t)(x.col * 3 + x.col) * Vh);
-        pf_l2(gb + (size_t)(x.c1 * 3 + x.col) * Vh);
-        pf_l2(gb + (size_t)(x.c2 * 3 + x.col) * Vh);
-    }
-}
-
-template <bool DAG, int WARPS>
-__global__ void __launch_bounds__(32 * WARPS) k_hop_df_pipe(const SplitDF p)
+// this thread's site, colour and shuffle partners (colour-split mapping)
+template <int WARPS>
+__device__ __forceinline__ SplitCtx split_ctx(const SplitDF &p)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int cq = lane / kSitesPerWarp;
@@ -179,6 +124,13 @@ __global__ void __launch_bounds__(32 * WARPS) k_hop_df_pipe(const SplitDF p)
     x.src1 = ls + kSitesPerWarp * x.c1;
     x.src2 = ls + kSitesPerWarp * x.c2;
     x.cs = wd_site(p.g, x.s, p.cb);
+    return x;
+}
+
+template <bool DAG, int WARPS>
+__global__ void __launch_bounds__(32 * WARPS) k_hop_df_pipe(const SplitDF p)
+{
+    const SplitCtx x = split_ctx<WARPS>(p);
     dfc acc[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfc());
@@ -214,43 +166,18 @@ __global__ void __launch_bounds__(32 * WARPS) k_hop_df_pipe(const SplitDF p)
     }
 }
 
-// Packed form (wd_df2.cuh): the same colour-split, software-pipelined
-// kernel with every double-float operation issued on (re, im) pairs -- half
-// the arithmetic instructions for the same FP32-pipe work, bit-identical
-// results.
+// Packed arithmetic (wd_df2.cuh): every double-float operation issued on
+// (re, im) pairs -- half the arithmetic instructions for the same FP32-pipe
+// work, lane by lane the roundings of the scalar form.
 struct DirLoadP {
     dfp s[4];
     dfp w[3];
 };
 
-__device__ __forceinline__ dfp ldp(const float4 *p, size_t i, bool on)
-{
-    return on ? dfp_from_f4(p[i]) : c_zero(dfp());
-}
-
 __device__ __forceinline__ dfp shfl_dfp(const dfp &v, int src)
 {
     return dfp{make_float2(__shfl_sync(kFull, v.h.x, src), __shfl_sync(kFull, v.h.y, src)),
                make_float2(__shfl_sync(kFull, v.l.x, src), __shfl_sync(kFull, v.l.y, src))};
-}
-
-template <int MU, bool FWD>
-__device__ __forceinline__ void pair_load(const SplitDF &p, const SplitCtx &x, DirLoadP &L)
-{
-    const size_t Vh = p.g.Vh;
-    const int nb = wd_neighbour(p.g, x.s, x.cs, MU, FWD);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) L.s[k] = ldp(p.in, (size_t)(k * 3 + x.col) * Vh + nb, x.on);
-    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? x.s : nb);
-    if constexpr (FWD) {
-        L.w[0] = ldp(gb, (size_t)(x.col * 3 + x.col) * Vh, x.on);
-        L.w[1] = ldp(gb, (size_t)(x.col * 3 + x.c1) * Vh, x.on);
-        L.w[2] = ldp(gb, (size_t)(x.col * 3 + x.c2) * Vh, x.on);
-    } else {
-        L.w[0] = ldp(gb, (size_t)(x.col * 3 + x.col) * Vh, x.on);
-        L.w[1] = ldp(gb, (size_t)(x.c1 * 3 + x.col) * Vh, x.on);
-        L.w[2] = ldp(gb, (size_t)(x.c2 * 3 + x.col) * Vh, x.on);
-    }
 }
 
 template <int MU, bool FWD, bool DAG>
@@ -272,71 +199,9 @@ __device__ __forceinline__ void pair_compute(const SplitCtx &x, const DirLoadP &
     wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
 }
 
-template <int MU, bool FWD, bool DAG>
-__device__ __forceinline__ void pair_dir(const SplitDF &p, const SplitCtx &x, dfp *acc)
+// out = alpha acc (+ beta x) for this thread's colour of its site
+__device__ __forceinline__ void pair_epilogue(const SplitDF &p, const SplitCtx &x, const dfp *acc)
 {
-    DirLoadP L;
-    pair_load<MU, FWD>(p, x, L);
-    pair_compute<MU, FWD, DAG>(x, L, acc);
-}
-
-// PIPE: loads of the next direction issued before the current one's
-// arithmetic (in registers); otherwise PF prefetches the next direction into
-// L2 instead (no registers held)
-template <bool DAG, int WARPS, bool PIPE, bool PF = false>
-__device__ __forceinline__ void hop_df_pair_body(const SplitDF &p)
-{
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int cq = lane / kSitesPerWarp;
-    const int ls = lane - cq * kSitesPerWarp;
-    const int s_raw = (blockIdx.x * WARPS + warp) * kSitesPerWarp + ls;
-    SplitCtx x;
-    x.on = cq < 3 && s_raw < p.g.Vh;
-    x.col = cq < 3 ? cq : 0;
-    x.s = x.on ? s_raw : 0;
-    x.c1 = x.col == 2 ? 0 : x.col + 1;
-    x.c2 = x.col == 0 ? 2 : x.col - 1;
-    x.src1 = ls + kSitesPerWarp * x.c1;
-    x.src2 = ls + kSitesPerWarp * x.c2;
-    x.cs = wd_site(p.g, x.s, p.cb);
-    dfp acc[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfp());
-    if constexpr (PIPE) {
-        DirLoadP A, B;
-        pair_load<0, true>(p, x, A);
-        pair_load<0, false>(p, x, B);
-        pair_compute<0, true, DAG>(x, A, acc);
-        pair_load<1, true>(p, x, A);
-        pair_compute<0, false, DAG>(x, B, acc);
-        pair_load<1, false>(p, x, B);
-        pair_compute<1, true, DAG>(x, A, acc);
-        pair_load<2, true>(p, x, A);
-        pair_compute<1, false, DAG>(x, B, acc);
-        pair_load<2, false>(p, x, B);
-        pair_compute<2, true, DAG>(x, A, acc);
-        pair_load<3, true>(p, x, A);
-        pair_compute<2, false, DAG>(x, B, acc);
-        pair_load<3, false>(p, x, B);
-        pair_compute<3, true, DAG>(x, A, acc);
-        pair_compute<3, false, DAG>(x, B, acc);
-    } else {
-        if constexpr (PF) split_prefetch<0, false>(p, x);
-        pair_dir<0, true, DAG>(p, x, acc);
-        if constexpr (PF) split_prefetch<1, true>(p, x);
-        pair_dir<0, false, DAG>(p, x, acc);
-        if constexpr (PF) split_prefetch<1, false>(p, x);
-        pair_dir<1, true, DAG>(p, x, acc);
-        if constexpr (PF) split_prefetch<2, true>(p, x);
-        pair_dir<1, false, DAG>(p, x, acc);
-        if constexpr (PF) split_prefetch<2, false>(p, x);
-        pair_dir<2, true, DAG>(p, x, acc);
-        if constexpr (PF) split_prefetch<3, true>(p, x);
-        pair_dir<2, false, DAG>(p, x, acc);
-        if constexpr (PF) split_prefetch<3, false>(p, x);
-        pair_dir<3, true, DAG>(p, x, acc);
-        pair_dir<3, false, DAG>(p, x, acc);
-    }
     if (!x.on) return;
     const size_t Vh = p.g.Vh;
     const dfp al{make_float2(p.alpha.h, p.alpha.h), make_float2(p.alpha.l, p.alpha.l)};
@@ -350,49 +215,110 @@ __device__ __forceinline__ void hop_df_pair_body(const SplitDF &p)
     }
 }
 
-template <bool DAG, int WARPS, bool PIPE, bool PF = false>
-__global__ void __launch_bounds__(32 * WARPS) k_hop_df_pair(const SplitDF p)
+// Staged packed form: each thread copies its own operands of the next LOOK
+// directions into shared memory with cp.async (no registers held while the
+// copies are in flight), then computes the current direction from shared
+// memory with the packed arithmetic (pair_compute: bit-identical to the other
+// forms).  A thread reads back only what it copied itself, so no block
+// barrier is needed: cp.async.wait_group makes a thread's completed copies
+// visible to it.  NS >= LOOK + 1 slots per thread; a slot is refilled
+// NS - LOOK directions after it was read.  Every address copied is one the
+// register-loading forms read (idle lanes use site 0), so all are in bounds.
+constexpr int kOps = 7;  // float4 operands per thread and direction: 4 spinor components, 3 link entries
+
+// L1-allocating copy (neighbour spinors: each is read by eight output sites)
+__device__ __forceinline__ void cp_async16(float4 *smem, const float4 *gmem)
 {
-    hop_df_pair_body<DAG, WARPS, PIPE, PF>(p);
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+// L2-only copy (links: each entry is read once per application)
+__device__ __forceinline__ void cp_async16_l2(float4 *smem, const float4 *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+template <bool L2ONLY>
+__device__ __forceinline__ void cp_async16_link(float4 *smem, const float4 *gmem)
+{
+    if constexpr (L2ONLY) cp_async16_l2(smem, gmem);
+    else cp_async16(smem, gmem);
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <bool DAG, int WARPS, int MINB>
-__global__ void __launch_bounds__(32 * WARPS, MINB) k_hop_df_split(const SplitDF p)
+// direction D = 2 mu + (0 forward, 1 backward): copy its operands into slot
+template <int D, bool LCG>
+__device__ __forceinline__ void stage_issue(const SplitDF &p, const SplitCtx &x, float4 *slot, int stride)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int cq = lane / kSitesPerWarp;          // 0..2, 3 for the two idle lanes
-    const int ls = lane - cq * kSitesPerWarp;     // site within the warp
-    const int s_raw = (blockIdx.x * WARPS + warp) * kSitesPerWarp + ls;
-    const bool on = cq < 3 && s_raw < p.g.Vh;
-    const int col = cq < 3 ? cq : 0;
-    const int s = on ? s_raw : 0;                 // idle lanes compute on site 0 and store nothing
-    const int c1 = col == 2 ? 0 : col + 1, c2 = col == 0 ? 2 : col - 1;
-    const int src1 = ls + kSitesPerWarp * c1, src2 = ls + kSitesPerWarp * c2;
-    const WdSite cs = wd_site(p.g, s, p.cb);
-    dfc acc[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfc());
-    split_dir<0, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    split_dir<0, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    split_dir<1, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    split_dir<1, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    split_dir<2, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    split_dir<2, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    split_dir<3, true, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    split_dir<3, false, DAG>(p, s, cs, col, c1, c2, src1, src2, on, acc);
-    if (!on) return;
+    constexpr int MU = D / 2;
+    constexpr bool FWD = (D % 2) == 0;
     const size_t Vh = p.g.Vh;
+    const int nb = wd_neighbour(p.g, x.s, x.cs, MU, FWD);
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const size_t i = (size_t)(k * 3 + col) * Vh + s;
-        dfc r{df_mul(p.alpha, acc[k].re), df_mul(p.alpha, acc[k].im)};
-        if (p.x) {
-            const dfc v = df_from_f4(p.x[i]);
-            r.re = df_madd(r.re, p.beta, v.re);
-            r.im = df_madd(r.im, p.beta, v.im);
-        }
-        p.out[i] = df_to_f4(r);
+    for (int k = 0; k < 4; ++k) cp_async16(slot + k * stride, p.in + (size_t)(k * 3 + x.col) * Vh + nb);
+    const float4 *gb = p.gauge + (size_t)((MU * 2 + (FWD ? p.cb : 1 - p.cb)) * 9) * Vh + (FWD ? x.s : nb);
+    if constexpr (FWD) {
+        cp_async16_link<LCG>(slot + 4 * stride, gb + (size_t)(x.col * 3 + x.col) * Vh);
+        cp_async16_link<LCG>(slot + 5 * stride, gb + (size_t)(x.col * 3 + x.c1) * Vh);
+        cp_async16_link<LCG>(slot + 6 * stride, gb + (size_t)(x.col * 3 + x.c2) * Vh);
+    } else {
+        cp_async16_link<LCG>(slot + 4 * stride, gb + (size_t)(x.col * 3 + x.col) * Vh);
+        cp_async16_link<LCG>(slot + 5 * stride, gb + (size_t)(x.c1 * 3 + x.col) * Vh);
+        cp_async16_link<LCG>(slot + 6 * stride, gb + (size_t)(x.c2 * 3 + x.col) * Vh);
     }
+}
+
+template <int D, bool DAG>
+__device__ __forceinline__ void stage_compute(const SplitCtx &x, const float4 *slot, int stride, dfp *acc)
+{
+    DirLoadP L;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) L.s[k] = dfp_from_f4(slot[k * stride]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) L.w[k] = dfp_from_f4(slot[(4 + k) * stride]);
+    pair_compute<D / 2, (D % 2) == 0, DAG>(x, L, acc);
+}
+
+template <int D, bool DAG, int LOOK, int NS, bool LCG>
+__device__ __forceinline__ void stage_step(const SplitDF &p, const SplitCtx &x, float4 *base, int stride, dfp *acc)
+{
+    if constexpr (D + LOOK < 8) stage_issue<D + LOOK, LCG>(p, x, base + ((D + LOOK) % NS) * kOps * stride, stride);
+    cp_async_commit();  // possibly empty: one group per step keeps the count
+    cp_async_wait<LOOK>();
+    stage_compute<D, DAG>(x, base + (D % NS) * kOps * stride, stride, acc);
+}
+
+template <bool DAG, int WARPS, int LOOK, int NS, bool LCG>
+__global__ void __launch_bounds__(32 * WARPS) k_hop_df_staged(const SplitDF p)
+{
+    static_assert(LOOK >= 1 && NS >= LOOK + 1, "slot count");
+    __shared__ float4 slots[NS * kOps * 32 * WARPS];
+    const SplitCtx x = split_ctx<WARPS>(p);
+    constexpr int stride = 32 * WARPS;
+    float4 *base = slots + threadIdx.x;
+    dfp acc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfp());
+    stage_issue<0, LCG>(p, x, base, stride);
+    cp_async_commit();
+    if constexpr (LOOK >= 2) {
+        stage_issue<1, LCG>(p, x, base + (1 % NS) * kOps * stride, stride);
+        cp_async_commit();
+    }
+    stage_step<0, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    stage_step<1, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    stage_step<2, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    stage_step<3, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    stage_step<4, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    stage_step<5, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    stage_step<6, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    stage_step<7, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+    pair_epilogue(p, x, acc);
 }
 
 __global__ void k_f64_to_df(const double2 *__restrict__ in, float4 *__restrict__ out, int64_t n)
@@ -429,15 +355,6 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
     p.out = out_block;
     p.alpha = df_split(alpha);
     p.beta = df_split(beta);
-    auto run = [&](auto warps, auto minb) -> wd_status {
-        constexpr int W = decltype(warps)::value, M = decltype(minb)::value;
-        const int sites_per_block = kSitesPerWarp * W;
-        const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
-        if (dag) k_hop_df_split<true, W, M><<<blocks, 32 * W, 0, ctx->stream>>>(p);
-        else k_hop_df_split<false, W, M><<<blocks, 32 * W, 0, ctx->stream>>>(p);
-        WD_LAUNCHED(ctx);
-        return WD_OK;
-    };
     auto run_pipe = [&](auto warps) -> wd_status {
         constexpr int W = decltype(warps)::value;
         const int sites_per_block = kSitesPerWarp * W;
@@ -447,36 +364,42 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
         WD_LAUNCHED(ctx);
         return WD_OK;
     };
-    auto run_pair = [&](auto warps, auto pf) -> wd_status {
+    auto run_staged = [&](auto warps, auto lcg) -> wd_status {
         constexpr int W = decltype(warps)::value;
-        constexpr bool PF = decltype(pf)::value;
+        constexpr bool LCG = decltype(lcg)::value;
         const int sites_per_block = kSitesPerWarp * W;
         const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
-        if (dag) k_hop_df_pair<true, W, false, PF><<<blocks, 32 * W, 0, ctx->stream>>>(p);
-        else k_hop_df_pair<false, W, false, PF><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        if (dag) k_hop_df_staged<true, W, 1, 2, LCG><<<blocks, 32 * W, 0, ctx->stream>>>(p);
+        else k_hop_df_staged<false, W, 1, 2, LCG><<<blocks, 32 * W, 0, ctx->stream>>>(p);
         WD_LAUNCHED(ctx);
         return WD_OK;
     };
-    // variants (ncu at 24^3x48 on GB300 in brackets): software-pipelined with 2
-    // and 4 warps per block [0.150 ms, 123.5 M warp instructions, 55 % FMA
-    // pipe, 68 % issue]; colour-split at <= 80 registers (6 blocks of 4 warps
-    // per SM); packed (re, im) pairs, 2 warps [0.163 ms: 87.7 M instructions
-    // but 6.6 long-scoreboard stalls per issue]; packed pairs with an L2
-    // prefetch of the next direction [0.153 ms, 100.9 M, stalls 3.5].  Every
-    // form tried lands at ~55 % of the FMA pipe.  Dropped: the unbounded
-    // colour-split form (242 registers, 0.225 ms), the register-prefetching
-    // packed form (0.180 ms), L2 prefetch on the scalar form (0.161 ms), the
-    // pipelined form capped at 80 or 72 registers (550-830 bytes of spills;
-    // 0.205 and 0.244 ms).
+    // Variants, D_eo on GB300 at 32^3x64 / 24^3x48 (CUDA events, best of 3x50):
+    //   0  staged, 4 warps, links copied L2-only   378.5 / 123.0 us
+    //   1  staged, 2 warps, links copied L2-only   383.2 / 123.3 us
+    //   2  staged, 2 warps, links through L1       386.2 / 127.0 us
+    //   3  register-pipelined scalar, 2 warps      459.9 / 150.1 us
+    //   4  register-pipelined scalar, 4 warps      459.0 / 149.5 us
+    // Dropped (same lattices): the staged form two directions ahead in three
+    // slots (413 / 135 us with L2-only links, 584 / 196 us through L1: the
+    // larger shared-memory footprint leaves less L1 for the neighbour
+    // spinors); staged with registers capped at 80 or 72 (420 and 635 us,
+    // spills); packed pairs loading into registers (504 us; 6.6
+    // long-scoreboard stalls per issue), with an L2 prefetch of the next
+    // direction (507 us); colour-split at <= 80 registers (478 us); the
+    // unbounded colour-split form (242 registers); the register-prefetching
+    // packed form; the scalar pipelined form capped at 80 or 72 registers
+    // (550-830 bytes of spills, 639 and 778 us).
     using F = std::false_type;
     using T = std::true_type;
     using W2 = std::integral_constant<int, 2>;
+    using W4 = std::integral_constant<int, 4>;
     return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 5, [&](int v) -> wd_status {
-        if (v == 1) return run_pipe(std::integral_constant<int, 4>());
-        if (v == 2) return run(std::integral_constant<int, 4>(), std::integral_constant<int, 6>());
-        if (v == 3) return run_pair(W2(), F());
-        if (v == 4) return run_pair(W2(), T());
-        return run_pipe(W2());
+        if (v == 1) return run_staged(W2(), T());
+        if (v == 2) return run_staged(W2(), F());
+        if (v == 3) return run_pipe(W2());
+        if (v == 4) return run_pipe(W4());
+        return run_staged(W4(), T());
     });
 }
 
