@@ -25,6 +25,7 @@
 #include "wd_hop.cuh"
 #include "wd_df.cuh"
 #include "wd_df2.cuh"
+#include "wd_async.cuh"
 #include "wd_kernels.h"
 #include <type_traits>
 #include "wd_tune.h"
@@ -226,29 +227,14 @@ __device__ __forceinline__ void pair_epilogue(const SplitDF &p, const SplitCtx &
 // register-loading forms read (idle lanes use site 0), so all are in bounds.
 constexpr int kOps = 7;  // float4 operands per thread and direction: 4 spinor components, 3 link entries
 
-// L1-allocating copy (neighbour spinors: each is read by eight output sites)
-__device__ __forceinline__ void cp_async16(float4 *smem, const float4 *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-// L2-only copy (links: each entry is read once per application)
-__device__ __forceinline__ void cp_async16_l2(float4 *smem, const float4 *gmem)
-{
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
+// spinors through L1 (each is read by eight output sites), links L2-only
+// (each entry is read once per application)
+__device__ __forceinline__ void cp_async16(float4 *smem, const float4 *gmem) { wd_cp_async_ca<16>(smem, gmem); }
 template <bool L2ONLY>
 __device__ __forceinline__ void cp_async16_link(float4 *smem, const float4 *gmem)
 {
-    if constexpr (L2ONLY) cp_async16_l2(smem, gmem);
-    else cp_async16(smem, gmem);
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait()
-{
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+    if constexpr (L2ONLY) wd_cp_async_cg16(smem, gmem);
+    else wd_cp_async_ca<16>(smem, gmem);
 }
 
 // direction D = 2 mu + (0 forward, 1 backward): copy its operands into slot
@@ -288,8 +274,8 @@ template <int D, bool DAG, int LOOK, int NS, bool LCG>
 __device__ __forceinline__ void stage_step(const SplitDF &p, const SplitCtx &x, float4 *base, int stride, dfp *acc)
 {
     if constexpr (D + LOOK < 8) stage_issue<D + LOOK, LCG>(p, x, base + ((D + LOOK) % NS) * kOps * stride, stride);
-    cp_async_commit();  // possibly empty: one group per step keeps the count
-    cp_async_wait<LOOK>();
+    wd_cp_async_commit();  // possibly empty: one group per step keeps the count
+    wd_cp_async_wait<LOOK>();
     stage_compute<D, DAG>(x, base + (D % NS) * kOps * stride, stride, acc);
 }
 
@@ -305,10 +291,10 @@ __global__ void __launch_bounds__(32 * WARPS) k_hop_df_staged(const SplitDF p)
 #pragma unroll
     for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfp());
     stage_issue<0, LCG>(p, x, base, stride);
-    cp_async_commit();
+    wd_cp_async_commit();
     if constexpr (LOOK >= 2) {
         stage_issue<1, LCG>(p, x, base + (1 % NS) * kOps * stride, stride);
-        cp_async_commit();
+        wd_cp_async_commit();
     }
     stage_step<0, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
     stage_step<1, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);

@@ -159,25 +159,14 @@ __device__ __forceinline__ void wd_recon(const C *t0, const C *t1, C *acc)
     for (int a = 0; a < 3; ++a) wd_recon1<MU, SG>(t0[a], t1[a], acc[a], acc[3 + a], acc[6 + a], acc[9 + a]);
 }
 
-// One of the eight neighbour terms (FIRST: the accumulators hold zeros).
-template <int MU, bool FWD, bool DAG, class P, bool FIRST = false>
-__device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, typename P::C *acc)
+// The terms of one of the eight neighbours from its spinor sp (site scale sc
+// when SCALED) and link matrix U (FIRST: the accumulators hold zeros).
+template <int MU, bool FWD, bool DAG, bool FIRST, bool SCALED, class C>
+__device__ __forceinline__ void wd_dir_terms(const C *sp, float sc, const C *U, C *acc)
 {
-    using C = typename P::C;
     constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
-    constexpr bool kScaled = wd_site_scaled<P>::value;
-    const int nb = wd_neighbour(p.g, s, c, MU, FWD);
-    C sp[12];
-    float sc = 1.f;
-    if constexpr (kScaled) sc = p.load_in_raw(nb, sp);
-    else p.load_in(nb, sp);
     C h0[3], h1[3];
     wd_proj<MU, SG>(sp, h0, h1);
-    C U[9];
-    // forward: U_mu(x) stored at this site (parity cb);
-    // backward: U_mu(x - mu) stored at the neighbour (parity 1-cb)
-    if constexpr (FWD) p.load_link(MU, p.cb, s, U);
-    else p.load_link(MU, 1 - p.cb, nb, U);
     C t0[3], t1[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -199,7 +188,7 @@ __device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, t
             }
         }
     }
-    if constexpr (kScaled) {
+    if constexpr (SCALED) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) wd_recon1_scaled<MU, SG>(t0[a], t1[a], sc, acc[a], acc[3 + a], acc[6 + a], acc[9 + a]);
     } else if constexpr (FIRST) {
@@ -208,6 +197,25 @@ __device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, t
     } else {
         wd_recon<MU, SG>(t0, t1, acc);
     }
+}
+
+// One of the eight neighbour terms (FIRST: the accumulators hold zeros).
+template <int MU, bool FWD, bool DAG, class P, bool FIRST = false>
+__device__ __forceinline__ void wd_hop_dir(const P &p, int s, const WdSite &c, typename P::C *acc)
+{
+    using C = typename P::C;
+    constexpr bool kScaled = wd_site_scaled<P>::value;
+    const int nb = wd_neighbour(p.g, s, c, MU, FWD);
+    C sp[12];
+    float sc = 1.f;
+    if constexpr (kScaled) sc = p.load_in_raw(nb, sp);
+    else p.load_in(nb, sp);
+    C U[9];
+    // forward: U_mu(x) stored at this site (parity cb);
+    // backward: U_mu(x - mu) stored at the neighbour (parity 1-cb)
+    if constexpr (FWD) p.load_link(MU, p.cb, s, U);
+    else p.load_link(MU, 1 - p.cb, nb, U);
+    wd_dir_terms<MU, FWD, DAG, FIRST, kScaled>(sp, sc, U, acc);
 }
 
 // 2 t - u, one rounding per real
