@@ -631,8 +631,6 @@ def run_ours(args) -> None:
             e1.record(stream)
             e1.synchronize()
             line["dslash_new_ms"] = e0.elapsed_time(e1) / n_full
-        line["autotune"] = [{"kernel": k, "half_volume": v, "variant": var, "ms": ms}
-                            for _, k, v, var, ms in wd.tune_report()]
         if not args.no_solver:
             line["solver"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, dims))}, "
                                           f"mass {MASS}, seed 2",
@@ -658,6 +656,10 @@ def run_ours(args) -> None:
                                           args.serve_requests_f64)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_port(gauge, src, dims)
+        # launch shapes the tuner chose for every kernel and size run above
+        # (half_volume: half-lattice sites, or a batch's system-sites rounded up to a power of 2)
+        line["autotune"] = [{"kernel": k, "half_volume": v, "variant": var, "ms": ms}
+                            for _, k, v, var, ms in wd.tune_report()]
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -96,38 +96,11 @@ __device__ __forceinline__ int find_group(const BGroup *groups, int ngroups, int
     return lo;
 }
 
-// SYS systems (warps) per block sharing the block's sites; MINB blocks per SM
-// (0: no bound) bound the registers (the kernel is latency-bound: DRAM bytes per
-// system-site sit at the link-shared minimum, so occupancy sets its speed)
-template <bool DAG, bool F16, int SYS, int MINB>
-__global__ void __launch_bounds__(kSites * SYS, MINB) k_batch_hop(const BTable t)
+// out = alpha acc (+ beta x) of system sys at site s (per-system scalars)
+template <bool F16>
+__device__ __forceinline__ void batch_epilogue(const BTable &t, const BSys &S, int sys, int s, int Vh,
+                                               const float2 *acc)
 {
-    const int gi = find_group(t.groups, t.ngroups, blockIdx.x);
-    const BGroup &G = t.groups[gi];
-    const int r = blockIdx.y * SYS + (threadIdx.x / kSites);
-    const int s = (blockIdx.x - G.block_start) * kSites + (threadIdx.x % kSites);
-    if (r >= G.nsys || s >= G.g.Vh) return;
-    const int sys = G.first_sys + r;
-    if (!t.active[sys]) return;
-    const BSys &S = t.sys[sys];
-    const int Vh = G.g.Vh;
-    float2 acc[12];
-    if constexpr (F16) {
-        BatchHop<SpF16, LinkF16> p;
-        p.g = G.g;
-        p.cb = t.cb;
-        p.in = SpF16{(uint4 *)S.in, S.in_scale, Vh};
-        const uint4 *a = (const uint4 *)G.gauge;
-        p.link = LinkF16{a, (const uint2 *)(a + (size_t)8 * Vh), Vh};
-        wd_hop_site<DAG>(p, s, acc);
-    } else {
-        BatchHop<SpF32, LinkF32> p;
-        p.g = G.g;
-        p.cb = t.cb;
-        p.in = SpF32{(float4 *)S.in, Vh};
-        p.link = LinkF32{(const float4 *)G.gauge, Vh};
-        wd_hop_site<DAG>(p, s, acc);
-    }
     const float al = t.alpha[sys], be = t.beta[sys];
     float2 r12[12];
     if (S.x) {
@@ -143,6 +116,48 @@ __global__ void __launch_bounds__(kSites * SYS, MINB) k_batch_hop(const BTable t
     }
     if constexpr (F16) SpF16{(uint4 *)S.out, S.out_scale, Vh}.store(s, r12);
     else SpF32{(float4 *)S.out, Vh}.store(s, r12);
+}
+
+// the operands of one system: its input spinor and the group's links
+template <bool F16>
+__device__ __forceinline__ auto batch_policy(const BTable &t, const BGroup &G, const BSys &S)
+{
+    const int Vh = G.g.Vh;
+    if constexpr (F16) {
+        BatchHop<SpF16, LinkF16> p;
+        p.g = G.g;
+        p.cb = t.cb;
+        p.in = SpF16{(uint4 *)S.in, S.in_scale, Vh};
+        const uint4 *a = (const uint4 *)G.gauge;
+        p.link = LinkF16{a, (const uint2 *)(a + (size_t)8 * Vh), Vh};
+        return p;
+    } else {
+        BatchHop<SpF32, LinkF32> p;
+        p.g = G.g;
+        p.cb = t.cb;
+        p.in = SpF32{(float4 *)S.in, Vh};
+        p.link = LinkF32{(const float4 *)G.gauge, Vh};
+        return p;
+    }
+}
+
+// SYS systems (warps) per block sharing the block's sites; MINB blocks per SM
+// (0: no bound) bound the registers (the kernel is latency-bound: DRAM bytes per
+// system-site sit at the link-shared minimum, so occupancy sets its speed)
+template <bool DAG, bool F16, int SYS, int MINB>
+__global__ void __launch_bounds__(kSites * SYS, MINB) k_batch_hop(const BTable t)
+{
+    const int gi = find_group(t.groups, t.ngroups, blockIdx.x);
+    const BGroup &G = t.groups[gi];
+    const int r = blockIdx.y * SYS + (threadIdx.x / kSites);
+    const int s = (blockIdx.x - G.block_start) * kSites + (threadIdx.x % kSites);
+    if (r >= G.nsys || s >= G.g.Vh) return;
+    const int sys = G.first_sys + r;
+    if (!t.active[sys]) return;
+    const BSys &S = t.sys[sys];
+    float2 acc[12];
+    wd_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
+    batch_epilogue<F16>(t, S, sys, s, G.g.Vh, acc);
 }
 
 // ---------------------------------------------------------- batched BLAS
@@ -645,7 +660,12 @@ wd_status BatchEngine::rebuild()
 }
 
 // batched hop h (operand table h) with launch variant v: (systems per block,
-// min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12), (4, none)
+// min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12), (4, none).  A whole
+// 24-source solve at 24^3x48 (GB300, seconds): FP32 inner 0.298 / 0.270 /
+// 0.265 / 0.268 / 0.274, FP16 inner 0.263 / 0.247 / 0.244 / 0.245 / 0.256.
+// Dropped: the hop with each thread's operands staged in shared memory by
+// cp.async, with 4 or 2 systems per block (FP32 0.276 / 0.279, FP16 0.243 /
+// 0.243: no gain; the block's systems already share links through L1).
 wd_status BatchEngine::hop(int h, int cb, int dag, int v)
 {
     const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_active_.p, cb};

@@ -8,8 +8,7 @@
 // ridge: FP32 runs at the HBM bound, FP16 (half the bytes, the same
 // arithmetic plus unpacking) at the instruction-issue bound.
 #include "wd_hop.cuh"
-#include "wd_lp.cuh"
-#include "wd_async.cuh"
+#include "wd_lp_staged.cuh"
 #include "wd_kernels.h"
 #include <type_traits>
 #include "wd_tune.h"
@@ -158,107 +157,42 @@ wd_status launch_hop(wd_context *ctx, const P &p, int dag)
     return WD_OK;
 }
 
-// FP16 kernel with each thread's operands of the next direction staged in
-// shared memory by cp.async while it computes the current direction from the
-// other slot (no registers held for the prefetch).  The decoding and the
-// arithmetic are those of the register-loading kernel (SpF16::load_raw,
-// LinkF16::load, wd_dir_terms), so the results are bit-identical.  A thread
-// reads back only the slots it filled itself: no block barrier.  Every
-// address copied is one the register-loading kernel reads.
-template <int T>
-struct F16Slots {
-    uint4 sp[2][3][T];  // spinor: 8 halves per entry
-    uint4 la[2][T];     // link complex 0..3
-    uint2 lb[2][T];     // link complex 4..5
-    float sc[2][T];     // spinor site scale
-};
-
-// direction D = 2 mu + (0 forward, 1 backward)
-template <int D, class P, int T>
-__device__ __forceinline__ void f16_stage(const P &p, int s, const WdSite &c, F16Slots<T> &S, int slot)
-{
-    constexpr int MU = D / 2;
-    constexpr bool FWD = (D % 2) == 0;
-    const int t = threadIdx.x;
-    const size_t Vh = p.g.Vh;
-    const int nb = wd_neighbour(p.g, s, c, MU, FWD);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) wd_cp_async_ca<16>(&S.sp[slot][j][t], p.in.p + (size_t)j * Vh + nb);
-    wd_cp_async_ca<4>(&S.sc[slot][t], p.in.scale + nb);
-    // forward: U_mu(x) at this site (parity cb); backward: U_mu(x - mu) at the neighbour
-    const size_t i = (size_t)(MU * 2 + (FWD ? p.cb : 1 - p.cb)) * Vh + (FWD ? s : nb);
-    wd_cp_async_cg16(&S.la[slot][t], p.link.a + i);
-    wd_cp_async_ca<8>(&S.lb[slot][t], p.link.b + i);
-}
-
-template <int D, bool DAG, int T>
-__device__ __forceinline__ void f16_compute(const F16Slots<T> &S, int slot, float2 *acc)
-{
-    const int t = threadIdx.x;
-    float2 sp[12], U[9];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) unpack4(S.sp[slot][j][t], sp + 4 * j);
-    const float sc = S.sc[slot][t];
-    unpack4(S.la[slot][t], U);
-    const uint2 v = S.lb[slot][t];
-    U[4] = h2f(*reinterpret_cast<const __half2 *>(&v.x));
-    U[5] = h2f(*reinterpret_cast<const __half2 *>(&v.y));
-    su3_row2(U);
-    wd_dir_terms<D / 2, (D % 2) == 0, DAG, false, true>(sp, sc, U, acc);
-}
-
-template <int D, bool DAG, class P, int T>
-__device__ __forceinline__ void f16_step(const P &p, int s, const WdSite &c, F16Slots<T> &S, float2 *acc)
-{
-    if constexpr (D + 1 < 8) f16_stage<D + 1>(p, s, c, S, (D + 1) & 1);
-    wd_cp_async_commit();  // possibly empty: one group per step keeps the count
-    wd_cp_async_wait<1>();
-    f16_compute<D, DAG>(S, D & 1, acc);
-}
-
+// the FP16 hopping kernel with the next direction's operands staged in
+// shared memory (wd_lp_staged.cuh)
 template <bool DAG, class P>
-__global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_f16_staged(const P p)
+__global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_lp_staged(const P p)
 {
-    constexpr int T = P::kThreads;
-    __shared__ F16Slots<T> S;
-    const int s = blockIdx.x * T + threadIdx.x;
+    using Sp = decltype(p.in);
+    using Lk = decltype(p.link);
+    __shared__ LpStage<Sp, Lk, P::kThreads> st;
+    const int s = blockIdx.x * P::kThreads + threadIdx.x;
     if (s >= p.g.Vh) return;
-    const WdSite c = wd_site(p.g, s, p.cb);
     float2 acc[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) acc[k] = c_zero(float2());
-    f16_stage<0>(p, s, c, S, 0);
-    wd_cp_async_commit();
-    f16_step<0, DAG>(p, s, c, S, acc);
-    f16_step<1, DAG>(p, s, c, S, acc);
-    f16_step<2, DAG>(p, s, c, S, acc);
-    f16_step<3, DAG>(p, s, c, S, acc);
-    f16_step<4, DAG>(p, s, c, S, acc);
-    f16_step<5, DAG>(p, s, c, S, acc);
-    f16_step<6, DAG>(p, s, c, S, acc);
-    f16_step<7, DAG>(p, s, c, S, acc);
+    lp_hop_site_staged<DAG>(p, s, acc, st);
     p.epilogue(s, acc);
 }
 
 template <class P>
-wd_status launch_hop_f16_staged(wd_context *ctx, const P &p, int dag)
+wd_status launch_hop_staged(wd_context *ctx, const P &p, int dag)
 {
     const int blocks = (p.g.Vh + P::kThreads - 1) / P::kThreads;
-    if (dag) k_hop_f16_staged<true><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
-    else k_hop_f16_staged<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+    if (dag) k_hop_lp_staged<true><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+    else k_hop_lp_staged<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
     WD_LAUNCHED(ctx);
     return WD_OK;
 }
 
 // the same operands in the launch variants the tuner times: 128, 64 or 256
 // threads per block, 128 with registers capped for 8 blocks per SM, and for
-// FP16 the cp.async-staged kernel with 128 or 64 threads.  GB300, D_eo at
-// 32^3x64 in us: FP16 75.1 / 75.8 / 80.0 / 73.8 / 71.8 / 71.9 (staged at
-// 48^3x96: 331 against 352); FP32 all within 1 % of 102.5.  Dropped: a
-// software-pipelined form issuing the next direction's register loads before
-// the current direction's arithmetic (76.1 and 102.4: the compiler already
-// hoists those loads), the staged FP16 kernel capped at 80 or 72 registers
-// (71.7-71.9, no gain).
+// FP16 the staged kernel with 128 or 64 threads (registers capped at 80).
+// GB300, D_eo at 32^3x64 in us: FP16 74.8 / 75.7 / 79.9 / 73.8 / 71.7 /
+// 71.8 (staged at 48^3x96: 331 against 352); FP32 all within 1 % of 102.5.
+// Dropped: the staged FP32 kernel (103.1-104.0: 144 bytes per thread and
+// slot leave less L1 for the neighbour spinors), the staged FP16 kernel
+// without the register cap (92-94 registers, 73.7), and a software-pipelined
+// form issuing the next direction's register loads before the current
+// direction's arithmetic (76.1 and 102.4: the compiler already hoists those
+// loads).
 template <class Sp, class Lk>
 wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p, int dag)
 {
@@ -274,8 +208,8 @@ wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p
         using T64 = std::integral_constant<int, 64>;
         using T128 = std::integral_constant<int, 128>;
         if constexpr (kF16) {
-            if (v == 4) return launch_hop_f16_staged(ctx, make(T128(), I0()), dag);
-            if (v == 5) return launch_hop_f16_staged(ctx, make(T64(), I0()), dag);
+            if (v == 4) return launch_hop_staged(ctx, make(T128(), std::integral_constant<int, 6>()), dag);
+            if (v == 5) return launch_hop_staged(ctx, make(T64(), std::integral_constant<int, 12>()), dag);
         }
         switch (v) {
         case 1: return launch_hop(ctx, make(T64(), I0()), dag);

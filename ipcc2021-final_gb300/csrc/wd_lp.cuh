@@ -13,6 +13,7 @@
 #include <cuda_fp16.h>
 #include "wd_internal.cuh"
 #include "wd_complex.cuh"
+#include "wd_async.cuh"
 
 __device__ __forceinline__ float2 h2f(__half2 h) { return __half22float2(h); }
 __device__ __forceinline__ __half2 f2h(float2 f) { return __float22half2_rn(f); }
@@ -88,6 +89,28 @@ struct SpF16 {
         for (int j = 0; j < 3; ++j) p[(size_t)j * Vh + s] = pack4(w + 4 * j);
         scale[s] = m;
     }
+    // shared-memory slot of T threads for the staged kernel (cp.async):
+    // stage() copies site s for thread t, unstage() decodes it as load_raw()
+    template <int T>
+    struct Slot {
+        uint4 v[3][T];
+        float sc[T];
+    };
+    template <int T>
+    __device__ __forceinline__ void stage(int s, Slot<T> &S, int t) const
+    {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) wd_cp_async_ca<16>(&S.v[j][t], p + (size_t)j * Vh + s);
+        wd_cp_async_ca<4>(&S.sc[t], scale + s);
+    }
+    // unscaled components (as load_raw); returns the site's scale
+    template <int T>
+    __device__ __forceinline__ float unstage(const Slot<T> &S, int t, float2 *v) const
+    {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) unpack4(S.v[j][t], v + 4 * j);
+        return S.sc[t];
+    }
 };
 
 inline SpF32 sp_f32(WdVec v, int Vh) { return SpF32{(float4 *)v.p, Vh}; }
@@ -132,6 +155,29 @@ struct LinkF16 {
         const size_t i = (size_t)(mu * 2 + par) * Vh + s;
         unpack4(__ldg(a + i), U);
         const uint2 v = __ldg(b + i);
+        U[4] = h2f(*reinterpret_cast<const __half2 *>(&v.x));
+        U[5] = h2f(*reinterpret_cast<const __half2 *>(&v.y));
+        su3_row2(U);
+    }
+    // staged copies: the 16-byte part L2-only (each link entry is read once
+    // per application; cp.async.cg takes 16 bytes only), the 8-byte part via L1
+    template <int T>
+    struct Slot {
+        uint4 a[T];
+        uint2 b[T];
+    };
+    template <int T>
+    __device__ __forceinline__ void stage(int mu, int par, int s, Slot<T> &S, int t) const
+    {
+        const size_t i = (size_t)(mu * 2 + par) * Vh + s;
+        wd_cp_async_cg16(&S.a[t], a + i);
+        wd_cp_async_ca<8>(&S.b[t], b + i);
+    }
+    template <int T>
+    __device__ __forceinline__ void unstage(const Slot<T> &S, int t, float2 *U) const
+    {
+        unpack4(S.a[t], U);
+        const uint2 v = S.b[t];
         U[4] = h2f(*reinterpret_cast<const __half2 *>(&v.x));
         U[5] = h2f(*reinterpret_cast<const __half2 *>(&v.y));
         su3_row2(U);

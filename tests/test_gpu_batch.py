@@ -74,3 +74,38 @@ def test_batch_rejects_fp64_inner(wd, ctx):
         ctx.solve_batch([(lat, lat.field(wd.gen_source(dims, 1)), lat.field(), 0.1)],
                         wd.solver_params(kind=wd.CG_EO, prec=wd.F64))
     assert e.value.status == wd.BAD_ARG
+
+
+@pytest.mark.parametrize("prec,kernel", [(2, "batch_hop_f32"), (3, "batch_hop_f16")])
+def test_batch_hop_variants_bit_identical(wd, ctx, prec, kernel):
+    """Every launch variant of the batched hop (the tuner picks one per batch
+    size) gives the same solutions bit for bit."""
+    dims, mass = (8, 4, 4, 8), 0.05
+    gauge = wd.gen_gauge(dims, seed=5)
+    lat = ctx.lattice(dims, gauge)
+    srcs = [wd.gen_source(dims, seed=200 + k) for k in range(6)]
+    fields = [(lat, lat.field(b), lat.field(), mass) for b in srcs]
+    params = wd.solver_params(kind=wd.CG_EO, mass=mass, tol=1e-10, max_iter=4000, prec=prec)
+    ctx.solve_batch(fields, params)  # registers the variant count
+    n = wd.tune_variants(kernel)
+    assert n >= 2
+    bucket = 1
+    while bucket < 6 * (int(np.prod(dims)) // 2):
+        bucket *= 2
+    ref = None
+    try:
+        for v in range(n):
+            wd.tune_pin(kernel, bucket, v)
+            for _, _, fx, _ in fields:
+                fx.zero()
+            stats = ctx.solve_batch(fields, params)
+            got = [fx.download() for _, _, fx, _ in fields]
+            its = [st.iterations for st in stats]
+            if ref is None:
+                ref = (got, its)
+            else:
+                assert its == ref[1], f"{kernel} variant {v}"
+                for a, b in zip(got, ref[0]):
+                    assert np.array_equal(a, b), f"{kernel} variant {v}"
+    finally:
+        wd.tune_pin(kernel, bucket, -1)
