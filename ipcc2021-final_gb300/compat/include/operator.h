@@ -20,16 +20,19 @@ static inline int get_nodenum(const int *x, int *l, int nd)
     return n;
 }
 
-// sum |A_i|^2 over the first / second half of a container
+// sum |A_i|^2 over the first / second half of a container.  Taken by
+// reference: the reference passes the container by value, which compiles
+// the same at every call site, but a copy of an owning container would free
+// its array twice (the containers here are not copyable).
 template <typename T>
-double norm_2_E(const T s)
+double norm_2_E(const T &s)
 {
     double r = 0.0;
     for (int i = 0; i < s.size / 2; ++i) r += std::norm(s.A[i]);
     return r;
 }
 template <typename T>
-double norm_2_O(const T s)
+double norm_2_O(const T &s)
 {
     double r = 0.0;
     for (int i = s.size / 2; i < s.size; ++i) r += std::norm(s.A[i]);
