@@ -65,6 +65,11 @@ wd_status wd_context_sync(wd_context *ctx);
 void *wd_context_stream(wd_context *ctx);
 /* Device kernels launched on this context since creation (bookkeeping for benchmarks). */
 uint64_t wd_context_launches(const wd_context *ctx);
+/* Testing aid, host-side failure injection: after n more successful field or
+ * work-buffer allocations on this context, the next ones fail with
+ * WD_ERR_OOM; n < 0 turns it off (the default).  Returns the previous
+ * setting (the allocations left before failing, or -1). */
+int wd_debug_fail_allocations_after(wd_context *ctx, int n);
 
 /* ---- gauge field (replaces lattice_gauge, include/lattice_gauge.h:11-26) ---- */
 /* Upload four reference-layout link arrays (each V*9 complex doubles).
@@ -198,7 +203,10 @@ wd_status wd_server_add_lattice(wd_server *server, const int dims[4], const doub
  * never fit the budget. */
 wd_status wd_server_submit(wd_server *server, int lattice_id, int nsrc, const double *const *sources,
                            const uint64_t *seeds, double mass, double tol, int64_t *request_id);
-/* admit queued requests that fit, advance every admitted system by one quantum, retire finished ones */
+/* admit queued requests that fit, advance every admitted system by one quantum, retire finished ones.
+ * A request whose admission fails (device allocation) leaves the queue with its unadmitted systems
+ * completed as failed (converged = 0, iterations = 0) and the error is returned; the server stays
+ * usable. */
 wd_status wd_server_step(wd_server *server, int *completed);
 /* done: 1 when finished; then solutions (nsrc host arrays, may be NULL), stats (nsrc) and the
  * submit-to-finish latency are returned and the request's device memory is released */

@@ -94,6 +94,7 @@ static void host_cache_drop(wd_context *ctx)
 
 wd_status wd_dev_alloc(wd_context *ctx, void **p, size_t bytes)
 {
+    if (wd_alloc_fails(ctx)) return wd_fail(ctx, WD_ERR_OOM, "work buffer: injected allocation failure");
     bytes = (bytes + 255) & ~(size_t)255;
     // best fit among cached blocks no more than twice the request
     auto it = ctx->pool_free.lower_bound(bytes);
@@ -165,6 +166,14 @@ extern "C" wd_status wd_context_sync(wd_context *ctx)
 }
 
 extern "C" void *wd_context_stream(wd_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" int wd_debug_fail_allocations_after(wd_context *ctx, int n)
+{
+    if (!ctx) return -1;
+    const int prev = ctx->fail_alloc_after;
+    ctx->fail_alloc_after = n < 0 ? -1 : n;
+    return prev;
+}
 extern "C" uint64_t wd_context_launches(const wd_context *ctx) { return ctx ? ctx->launches : 0; }
 
 static wd_status ensure_staging(wd_context *ctx, size_t bytes)
@@ -269,6 +278,7 @@ extern "C" wd_status wd_field_create_prec(wd_context *ctx, const wd_lattice *lat
     if (!ctx || !lat || !out) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
     if (prec < WD_PREC_F64 || prec > WD_PREC_F16) return wd_fail(ctx, WD_ERR_BAD_ARG, "unknown precision");
     *out = nullptr;
+    if (wd_alloc_fails(ctx)) return wd_fail(ctx, WD_ERR_OOM, "field: injected allocation failure");
     wd_field *f = new wd_field();
     f->lat = lat;
     f->storage = prec;

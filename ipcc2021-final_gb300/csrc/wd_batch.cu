@@ -1052,9 +1052,28 @@ static wd_status server_source(wd_server *sv, const wd_server::Pending &p, int k
     return wd_blas_scale(ctx, v.x > 0 ? 1.0 / std::sqrt(v.x) : 1.0, f->d, f->d, n);
 }
 
-static wd_status server_admit(wd_server *sv)
+// systems k0.. of request r that could not be admitted complete as failed
+// (not converged, no iterations), so the request still finishes
+static void server_fail_from(wd_server::Req &r, int k0, int *completed)
 {
-    wd_status st;
+    for (int k = k0; k < r.nsrc; ++k) r.st[k] = wd_solver_stats{};
+    r.remaining -= r.nsrc - k0;
+    if (r.remaining == 0) {
+        r.done = true;
+        r.t_done = std::chrono::steady_clock::now();
+        for (wd_field *f : r.src) wd_field_destroy(f);
+        r.src.clear();
+        ++*completed;
+    }
+}
+
+// Admits queued requests in order while the HBM budget and the slot count
+// allow.  A request's fields and sources are created first, all or none; an
+// allocation failure fails the whole request, a failure while handing its
+// systems to the solver fails the systems not yet handed over.  Either way
+// the request leaves the queue and the error is returned.
+static wd_status server_admit(wd_server *sv, int *completed)
+{
     while (!sv->queue.empty()) {
         wd_server::Pending &p = sv->queue.front();
         const wd_lattice *lat = sv->lats[p.lat];
@@ -1062,25 +1081,42 @@ static wd_status server_admit(wd_server *sv)
         if (sv->gauge_bytes + sv->req_bytes + bytes > sv->cfg.hbm_budget_bytes) break;
         if (sv->active_systems > 0 && sv->active_systems + p.nsrc > sv->cfg.max_systems) break;
         wd_server::Req &r = sv->reqs[p.id];
-        r.bytes = bytes;
-        sv->req_bytes += bytes;
-        for (int k = 0; k < p.nsrc; ++k) {
+        wd_status st = WD_OK;
+        for (int k = 0; k < p.nsrc && st == WD_OK; ++k) {
             wd_field *fs = nullptr, *fd = nullptr;
-            if ((st = wd_field_create(sv->ctx, lat, &fs)) != WD_OK) return st;
-            r.src.push_back(fs);
-            if ((st = wd_field_create(sv->ctx, lat, &fd)) != WD_OK) return st;
-            r.dest.push_back(fd);
-            if ((st = server_source(sv, p, k, fs)) != WD_OK) return st;
-            const int tag = sv->next_tag++;
-            sv->tag_req[tag] = {p.id, k};
-            sv->active_systems++;
-            if (sv->eng) {
-                if ((st = sv->eng->add(tag, lat, fs->d, fd->d, p.mass, p.tol)) != WD_OK) return st;
-            } else {
-                sv->fp64_todo.push_back(tag);
+            st = wd_field_create(sv->ctx, lat, &fs);
+            if (st == WD_OK) {
+                r.src.push_back(fs);
+                st = wd_field_create(sv->ctx, lat, &fd);
+            }
+            if (st == WD_OK) {
+                r.dest.push_back(fd);
+                st = server_source(sv, p, k, fs);
             }
         }
+        if (st != WD_OK) {
+            for (wd_field *f : r.dest) wd_field_destroy(f);
+            r.dest.clear();
+            server_fail_from(r, 0, completed);
+            sv->queue.pop_front();
+            return st;
+        }
+        r.bytes = bytes;
+        sv->req_bytes += bytes;
+        int k = 0;
+        for (; k < p.nsrc; ++k) {
+            const int tag = sv->next_tag++;
+            if (sv->eng) st = sv->eng->add(tag, lat, r.src[k]->d, r.dest[k]->d, p.mass, p.tol);
+            if (st != WD_OK) break;
+            if (!sv->eng) sv->fp64_todo.push_back(tag);
+            sv->tag_req[tag] = {p.id, k};
+            sv->active_systems++;
+        }
         sv->queue.pop_front();
+        if (st != WD_OK) {
+            server_fail_from(r, k, completed);
+            return st;
+        }
     }
     return WD_OK;
 }
@@ -1106,8 +1142,11 @@ extern "C" wd_status wd_server_step(wd_server *sv, int *completed)
 {
     if (!sv) return WD_ERR_BAD_ARG;
     int done = 0;
-    wd_status st = server_admit(sv);
-    if (st != WD_OK) return st;
+    wd_status st = server_admit(sv, &done);
+    if (st != WD_OK) {
+        if (completed) *completed = done;
+        return st;
+    }
     std::vector<int> fin;
     if (sv->eng) {
         sv->eng->take_retired(&fin);  // systems already solved at admission
@@ -1144,7 +1183,9 @@ extern "C" wd_status wd_server_poll(wd_server *sv, int64_t id, int *done, double
     if (!r.done) return WD_OK;
     wd_status st = WD_OK;
     for (int k = 0; k < r.nsrc; ++k) {
-        if (solutions && solutions[k] && st == WD_OK) st = wd_field_download(sv->ctx, r.dest[k], solutions[k]);
+        // a request that failed admission has no solution fields: its solutions stay untouched
+        if (solutions && solutions[k] && k < (int)r.dest.size() && st == WD_OK)
+            st = wd_field_download(sv->ctx, r.dest[k], solutions[k]);
         if (stats) stats[k] = r.st[k];
     }
     if (latency_s) *latency_s = std::chrono::duration<double>(r.t_done - r.t_submit).count();

@@ -56,7 +56,20 @@ struct wd_context {
     std::multimap<size_t, void *> pool_free;
     std::unordered_map<void *, size_t> pool_used;
     size_t pool_bytes = 0;
+    // host-side failure injection for tests: after this many more successful
+    // field / work-buffer allocations the next ones fail with WD_ERR_OOM
+    // (-1: off)
+    int fail_alloc_after = -1;
 };
+
+// true when the injected allocation failure applies to this allocation
+inline bool wd_alloc_fails(wd_context *ctx)
+{
+    if (ctx->fail_alloc_after < 0) return false;
+    if (ctx->fail_alloc_after == 0) return true;
+    --ctx->fail_alloc_after;
+    return false;
+}
 
 // Work-buffer allocation through the context's cache (stream-ordered reuse;
 // on allocation failure the cached blocks are released and the call retried).

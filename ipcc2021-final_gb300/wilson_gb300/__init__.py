@@ -73,6 +73,7 @@ def _load() -> C.CDLL:
         "wd_context_sync": (C.c_int, [vp]),
         "wd_context_stream": (vp, [vp]),
         "wd_context_launches": (C.c_uint64, [vp]),
+        "wd_debug_fail_allocations_after": (C.c_int, [vp, C.c_int]),
         "wd_lattice_create": (C.c_int, [vp, ip, d4, C.POINTER(vp)]),
         "wd_lattice_update": (C.c_int, [vp, vp, d4]),
         "wd_lattice_destroy": (None, [vp]),
@@ -254,6 +255,11 @@ class Context:
     @property
     def launches(self) -> int:
         return int(lib.wd_context_launches(self.handle))
+
+    def fail_allocations_after(self, n: int) -> int:
+        """Testing aid: the next allocations after n more successful ones fail
+        with OOM (n < 0: off).  Returns the previous setting."""
+        return int(lib.wd_debug_fail_allocations_after(self.handle, int(n)))
 
     def fma_peak(self) -> tuple[float, float]:
         """Measured (FP64, FP32) FMA throughput of the device in TFLOP/s."""

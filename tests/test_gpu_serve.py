@@ -117,3 +117,38 @@ def test_budget_admission_and_fp64_mode(wd, ctx, oracle, gauges):
     for rid_mixed, rid64 in zip(sorted(res), sorted(res64)):
         assert rel_l2(res[rid_mixed][0][0], res64[rid64][0][0]) <= 100 * 1e-10
     sv.close()
+
+
+def test_admission_failure_completes_request_and_server_stays_usable(wd, ctx, oracle, gauges):
+    """A request whose admission fails (allocation failure injected on the
+    host) leaves the queue with its systems completed as failed, step reports
+    OOM, and the server keeps serving."""
+    sv, ids = make_server(wd, ctx, gauges, prec=wd.F32)
+    try:
+        # (a) the second of the request's fields fails: nothing is admitted
+        ra = sv.submit(ids[0], 3, mass=0.1, tol=1e-10, seeds=[1, 2, 3])
+        ctx.fail_allocations_after(1)
+        with pytest.raises(wd.WilsonError) as e:
+            sv.step()
+        ctx.fail_allocations_after(-1)
+        assert e.value.status == wd.OOM
+        done, sols, stats, _ = sv.poll(ra)
+        assert done and all(s.converged == 0 and s.iterations == 0 for s in stats)
+        # (b) every field is created, then handing the first system to the solver fails
+        rb = sv.submit(ids[0], 3, mass=0.1, tol=1e-10, seeds=[1, 2, 3])
+        ctx.fail_allocations_after(2 * 3 + 1)
+        with pytest.raises(wd.WilsonError) as e:
+            sv.step()
+        ctx.fail_allocations_after(-1)
+        assert e.value.status == wd.OOM
+        done, sols, stats, _ = sv.poll(rb, want_solutions=True)
+        assert done and all(s.converged == 0 for s in stats)
+        q, active, _ = sv.status()
+        assert q == 0 and active == 0
+        # (c) the server still serves
+        rc = sv.submit(ids[1], 2, mass=0.1, tol=1e-10, seeds=[7, 8])
+        out = drain(sv, [rc])
+        assert all(s.converged and s.true_residual <= 1e-10 for s in out[rc][1])
+    finally:
+        ctx.fail_allocations_after(-1)
+        sv.close()
