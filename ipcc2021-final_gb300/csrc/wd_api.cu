@@ -622,47 +622,55 @@ static wd_status host_pipeline(wd_context *ctx, const double *src, double *dest,
         }
         return WD_OK;
     };
-    // uploads start after the work already queued on the context's stream
-    WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[0], ctx->stream));
-    WD_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d_stream, ctx->chunk_done[0], 0));
-    // chunks 1..n-1, then 0; consecutive chunks alternate between two compute
-    // streams, so one chunk's last partial wave of blocks overlaps the next's first
-    for (int i = 0; i < n; ++i) {
-        const int j = n == 1 ? 0 : (i + 1) % n;
-        const int need = (j == 0 || tb[j + 1] >= Lt) ? nu - 1 : tb[j + 1] / us;
-        if ((st = upload_through(need)) != WD_OK) return st;
-        cudaStream_t cs = (i & 1) ? ctx->aux_stream : ctx->stream;
-        WD_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->chunk_in[need], 0));
-        const int lo = tb[j] * slab, hi = tb[j + 1] * slab;
-        for (int p = 0; p < 2; ++p)
-            if (out_mask & (1 << p))
-                if ((st = compute(cs, p, lo, hi, in_aos, out_aos)) != WD_OK) return st;
-        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[j], cs));
-        WD_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[j], 0));
-        for (int p = 0; p < 2; ++p)
-            if (out_mask & (1 << p))
-                if ((st = move((double2 *)dest + p * half + (size_t)lo * 12, out_aos + p * half + (size_t)lo * 12,
-                               (size_t)(hi - lo) * 12, cudaMemcpyDeviceToHost, dest_direct, ctx->copy_stream)) !=
-                    WD_OK)
-                    return st;
-    }
+    auto enqueue = [&]() -> wd_status {
+        // uploads start after the work already queued on the context's stream
+        WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[0], ctx->stream));
+        WD_CUDA(ctx, cudaStreamWaitEvent(ctx->h2d_stream, ctx->chunk_done[0], 0));
+        // chunks 1..n-1, then 0; consecutive chunks alternate between two compute
+        // streams, so one chunk's last partial wave of blocks overlaps the next's first
+        for (int i = 0; i < n; ++i) {
+            const int j = n == 1 ? 0 : (i + 1) % n;
+            const int need = (j == 0 || tb[j + 1] >= Lt) ? nu - 1 : tb[j + 1] / us;
+            if ((st = upload_through(need)) != WD_OK) return st;
+            cudaStream_t cs = (i & 1) ? ctx->aux_stream : ctx->stream;
+            WD_CUDA(ctx, cudaStreamWaitEvent(cs, ctx->chunk_in[need], 0));
+            const int lo = tb[j] * slab, hi = tb[j + 1] * slab;
+            for (int p = 0; p < 2; ++p)
+                if (out_mask & (1 << p))
+                    if ((st = compute(cs, p, lo, hi, in_aos, out_aos)) != WD_OK) return st;
+            WD_CUDA(ctx, cudaEventRecord(ctx->chunk_done[j], cs));
+            WD_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[j], 0));
+            for (int p = 0; p < 2; ++p)
+                if (out_mask & (1 << p))
+                    if ((st = move((double2 *)dest + p * half + (size_t)lo * 12, out_aos + p * half + (size_t)lo * 12,
+                                   (size_t)(hi - lo) * 12, cudaMemcpyDeviceToHost, dest_direct, ctx->copy_stream)) !=
+                        WD_OK)
+                        return st;
+        }
+        return WD_OK;
+    };
+    st = enqueue();
     // a parity of dest the operator does not write is zero.  Four threads: the
     // copies to and from host memory run meanwhile, and a wider team both
     // competes with them for host memory bandwidth and, on a busy host, waits
     // on descheduled threads (measured at 32^3x64: 2.03 ms per call with 2-8
     // threads, up to 4.4 ms with 16 on 16 cores).
-    for (int p = 0; p < 2; ++p)
+    for (int p = 0; p < 2 && st == WD_OK; ++p)
         if (!(out_mask & (1 << p))) {
             double *zero = dest + (size_t)p * half * 2;
             const int64_t nz = (int64_t)half * 2;
 #pragma omp parallel for schedule(static) num_threads(4)
             for (int64_t i = 0; i < nz; ++i) zero[i] = 0.0;
         }
-    WD_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
-    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    WD_CUDA(ctx, cudaStreamSynchronize(ctx->aux_stream));
-    WD_CUDA(ctx, cudaStreamSynchronize(ctx->h2d_stream));
-    return WD_OK;
+    // drain every stream the pipeline used -- after an enqueue error too, so
+    // that no copy or kernel still reads src or writes dest once the call
+    // returns and the caller may free them
+    const cudaStream_t used[4] = {ctx->copy_stream, ctx->stream, ctx->aux_stream, ctx->h2d_stream};
+    for (cudaStream_t q : used) {
+        const cudaError_t e = cudaStreamSynchronize(q);
+        if (e != cudaSuccess && st == WD_OK) st = wd_cuda_check(ctx, e, "cudaStreamSynchronize");
+    }
+    return st;
 }
 
 // DslashoffdNew on host arrays: only the source parity the term reads (1-cb)
