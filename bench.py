@@ -59,6 +59,17 @@ FLOPS_PER_SITE = 1320
 METRIC = "Dslash GB/s at 32^3x64 (even-odd D_eo, FP64, compulsory bytes)"
 
 
+def workload_config(dims, prec: str = "f64") -> dict:
+    """The `config` of the benchmark line, the same dict in both arms."""
+    V = int(np.prod(dims))
+    links, spinor = 4 * V * 9 * 16, V // 2 * 12 * 16
+    return {"workload": f"even-odd Dslash D_eo, {'x'.join(map(str, dims))}, seed 2, {prec.upper()} "
+                        f"(repeated applications)",
+            "lattice": list(dims), "sites": V, "precision": prec,
+            "l2": f"inputs larger than L2, no flush ({links / 1e9:.2f} GB links + {spinor / 1e6:.0f} MB "
+                  f"spinor per parity; L2 129 MB)"}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -129,18 +140,13 @@ def measured_peak_hbm() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def profiled_traffic(name: str):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
-    p = REPO / "profiles" / name
-    if not p.exists():
-        return None
-    for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1])
-            except ValueError:
-                return None
-    return None
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per D_eo launch
+# at 32^3x64, from one ncu capture of each kernel at 24^3x48 scaled by the
+# number of output sites (traffic per site is constant across volumes for
+# these kernels); not measured by this run.
+TRAFFIC_PER_LAUNCH = {"f64": 1.595e9, "df64": 1.591e9, "f32": 5.660e8, "f16": 2.731e8}
+TRAFFIC_SOURCE = ("ncu capture at 24^3x48 of the same kernel (dram__bytes_read.sum + dram__bytes_write.sum), "
+                  "scaled to 32^3x64 by output sites; a recorded constant, not measured in this run")
 
 
 def cpu_baseline_port(gauge, src, dims, seconds: float = 12.0) -> dict:
@@ -251,11 +257,40 @@ def small_config_bench(wd, ctx, with_cpu: bool) -> dict:
 SOLVER_PLANS = ("f64", "df64", "mixed_f32", "mixed_f16", "mixed_f16_df64")
 
 
+class OracleSolution:
+    """The oracle's solution of one solver workload, computed on the host cores
+    before the GPU solves and outside every timed region: even-odd CG driven
+    to a normal residual of 1e-14 (FP64 true residual ~1e-13)."""
+
+    def __init__(self, gauge, src, dims, mass: float):
+        sys.path.insert(0, str(REPO / "oracle"))
+        from oracle import Oracle
+
+        self.orc = Oracle()
+        self.cores = self.orc.threads(os.cpu_count() or 1)
+        self.gauge, self.src, self.dims, self.mass = gauge, src, dims, mass
+        t0 = time.perf_counter()
+        self.x, self.iterations, self.true_residual = self.orc.cg_eo(src, gauge, dims, mass, tol=1e-14)
+        self.seconds = time.perf_counter() - t0
+
+    def judge(self, sol) -> dict:
+        """Error of a GPU solution against this one, and its FP64 true residual
+        recomputed by the oracle."""
+        r = self.src - self.orc.dslash_full(sol, self.gauge, self.dims, self.mass, 0)
+        return {"err_vs_oracle": float(np.linalg.norm(sol - self.x) / np.linalg.norm(self.x)),
+                "true_residual_oracle": float(np.linalg.norm(r) / np.linalg.norm(self.src))}
+
+    def summary(self) -> dict:
+        return {"solver": "even-odd CG on the host cores, normal residual 1e-14", "cores": self.cores,
+                "iterations": self.iterations, "seconds": self.seconds, "true_residual": self.true_residual}
+
+
 def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10, plans=SOLVER_PLANS,
-                 profile: bool = False) -> dict:
+                 profile: bool = False, oracle_sol: OracleSolution | None = None) -> dict:
     """Solves per arithmetic on the resident lattice (the median of three timed
-    solves after a warm-up): solves/s, iterations, FP64 true residual, and the
-    relative difference to the FP64 solution.
+    solves after a warm-up): solves/s, iterations, FP64 true residual, the
+    relative difference to the FP64 solution and, given the oracle's solution,
+    the error against it and the true residual the oracle recomputes.
     profile=True brackets each timed solve with cudaProfilerStart/Stop (for
     `ncu --profile-from-start off`)."""
     import torch
@@ -287,11 +322,15 @@ def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10, plans=SOLVE
         out[name] = {"solves_per_s": 1.0 / secs, "seconds": secs, "seconds_each": times, "iterations": st.iterations,
                      "reliable_updates": st.reliable_updates, "true_residual": st.true_residual,
                      "rel_diff_vs_f64": float(np.linalg.norm(sol - ref) / np.linalg.norm(ref))}
+        if oracle_sol is not None:
+            out[name].update(oracle_sol.judge(sol))
         x.close()
     if "f64" in out:
         for name in out:
             if name != "f64":
                 out[name]["speedup_vs_f64"] = out["f64"]["seconds"] / out[name]["seconds"]
+    if oracle_sol is not None:
+        out["oracle"] = oracle_sol.summary()
     return out
 
 
@@ -438,7 +477,9 @@ def serve_run(wd, ctx, reqs, rate: float, prec: int, budget: float = 150e9, seed
     return {"rate_req_per_s": rate, "requests": len(reqs), "solves": solves, "wall_s": wall,
             "solves_per_s": solves / wall, "requests_per_s": len(reqs) / wall,
             "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
-            "max_residual_over_tol": worst}
+            "max_residual_over_tol": worst,
+            # served below 90 % of the offered rate: the server is the bottleneck
+            "saturated": bool(len(reqs) / wall < 0.9 * rate)}
 
 
 def serve_bench(wd, ctx, n: int, rates_mixed, rates_f64, n_f64: int | None = None) -> dict:
@@ -451,6 +492,11 @@ def serve_bench(wd, ctx, n: int, rates_mixed, rates_f64, n_f64: int | None = Non
                        "1-12 sources, 8 resident gauge fields, 150 GB budget",
            "mixed_batched_f32": [serve_run(wd, ctx, reqs, r, wd.F32) for r in rates_mixed],
            "plain_f64": [serve_run(wd, ctx, reqs64, r, wd.F64) for r in rates_f64]}
+    sat = {k: max((r["solves_per_s"] for r in out[k] if r["saturated"]), default=None)
+           for k in ("mixed_batched_f32", "plain_f64")}
+    out["saturated_solves_per_s"] = sat
+    if sat["mixed_batched_f32"] and sat["plain_f64"]:
+        out["saturated_ratio_mixed_vs_f64"] = sat["mixed_batched_f32"] / sat["plain_f64"]
     return out
 
 
@@ -473,17 +519,18 @@ def replica_throughput(units_per_rank: float, seconds_max: float, world: int) ->
 
 
 def run_reference(args) -> None:
+    """The reference's CPU implementation of the path on the host cores, on
+    the same workload: only the oracle's host library is loaded (its copy of
+    the seeded generator gives the GPU arm's input bytes)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import wilson_gb300 as wd
-
-    gauge = wd.gen_gauge(DIMS, SEED, EPS)
-    src = wd.gen_source(DIMS, SEED)
     sys.path.insert(0, str(REPO / "oracle"))
     from oracle import Oracle
 
     orc = Oracle()
+    gauge = orc.gen_gauge(DIMS, SEED, EPS)
+    src = orc.gen_source(DIMS, SEED)
     cores = orc.threads(os.cpu_count() or 1)
     vh = int(np.prod(DIMS)) // 2
     orc.dslash_offd(src, gauge, DIMS, 0, 0)  # warm-up (page in, thread pool)
@@ -500,10 +547,8 @@ def run_reference(args) -> None:
     line = {"metric": METRIC, "value": v, "unit": "GB/s", "n_gpus": world, "steps": n, "warmup": args.warmup,
             "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded SU(3) links eps=0.5, unit Gaussian source)",
-            "config": {"workload": f"even-odd Dslash D_eo, {'x'.join(map(str, DIMS))}, seed 2 "
-                                   f"({n} repeated applications)",
-                       "lattice": list(DIMS), "sites": int(np.prod(DIMS)), "precision": "f64",
-                       "parallelism": f"host threads x{cores}"},
+            "config": workload_config(DIMS),
+            "parallelism": f"host threads x{cores}",
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "GB/s", "cores": cores, "kind": "port",
                              "sample": f"{n} DslashoffdNew applications at 32x32x32x64 (C restatement of the "
@@ -596,21 +641,19 @@ def run_ours(args) -> None:
         fp64_peak, fp32_peak = ctx.fma_peak()
         achieved = bps * vh / (ms * 1e-3) / 1e9
         gflops = FLOPS_PER_SITE * vh / (ms * 1e-3) / 1e9
-        traffic = profiled_traffic(f"dslash_{args.prec}_32c64.md")
+        traffic = TRAFFIC_PER_LAUNCH[args.prec] if dims == DIMS else None
         line = {
             "metric": METRIC if args.prec == "f64" else METRIC.replace("FP64", args.prec.upper()), "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.prec,
             "data": "synthetic (seeded SU(3) links eps=0.5, unit Gaussian source)",
-            "config": {"workload": f"even-odd Dslash D_eo, {'x'.join(map(str, dims))}, seed 2 "
-                                   f"({args.steps} repeated applications)",
-                       "lattice": list(dims), "sites": int(np.prod(dims)), "precision": args.prec,
-                       "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (1.2 GB links + 201 MB spinor per parity)"},
+            "config": workload_config(dims, args.prec),
+            "parallelism": f"replicas x{world}",
             "gflops": gflops * world,
             "effective_gbs_quda_style": 2880 * vh / (ms * 1e-3) / 1e9,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "frac": achieved / peak, "traffic": traffic, "traffic_source": TRAFFIC_SOURCE,
+                         "peak_source": peak_src,
                          "note": "FP64 kernels are bounded by the FP64 pipe on GB300; see compute"},
             "compute": {"bound": "fp64" if args.prec == "f64" else "fp32",
                         "achieved_tflops": gflops / 1e3,
@@ -633,22 +676,29 @@ def run_ours(args) -> None:
             e1.record(stream)
             e1.synchronize()
             line["dslash_new_ms"] = e0.elapsed_time(e1) / n_full
+        with_oracle = not args.no_cpu_baseline
         if not args.no_solver:
+            osol = OracleSolution(gauge, src, dims, MASS) if with_oracle else None
             line["solver"] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, dims))}, "
                                           f"mass {MASS}, seed 2",
                               **solver_bench(wd, ctx, lat, src, MASS, plans=args.solver_plans,
-                                             profile=args.profile_solves)}
+                                             profile=args.profile_solves, oracle_sol=osol)}
+            del osol
         if not args.no_solver_mixed:
             # the mixed-precision configuration: mass 0.01 on 32^3x64 and on 48^3x96
             for key, sd in (("solver_mixed", tuple(args.solver_dims)), ("solver_mixed_large", (48, 48, 48, 96))):
                 if key == "solver_mixed_large" and args.no_solver_large:
                     continue
-                slat = ctx.lattice(sd, wd.gen_gauge(sd, SEED, EPS))
+                sgauge = gauge if sd == dims else wd.gen_gauge(sd, SEED, EPS)
+                ssrc = src if sd == dims else wd.gen_source(sd, SEED)
+                osol = OracleSolution(sgauge, ssrc, sd, args.solver_mass) if with_oracle else None
+                slat = ctx.lattice(sd, sgauge)
                 line[key] = {"workload": f"even-odd CG to true residual 1e-10, {'x'.join(map(str, sd))}, "
                                          f"mass {args.solver_mass}, seed 2",
-                             **solver_bench(wd, ctx, slat, wd.gen_source(sd, SEED), args.solver_mass,
-                                            plans=args.solver_plans, profile=args.profile_solves)}
+                             **solver_bench(wd, ctx, slat, ssrc, args.solver_mass,
+                                            plans=args.solver_plans, profile=args.profile_solves, oracle_sol=osol)}
                 slat.close()
+                del osol, sgauge, ssrc
         if not args.no_solver:
             line["small_config"] = small_config_bench(wd, ctx, not args.no_cpu_baseline)
         if not args.no_batch:
@@ -689,14 +739,15 @@ def main() -> None:
     ap.add_argument("--solver-mass", type=float, default=0.01)
     ap.add_argument("--no-solver-mixed", action="store_true", help="skip the mass-0.01 solver measurements")
     ap.add_argument("--no-solver-large", action="store_true", help="skip the 48^3x96 solver measurement")
-    ap.add_argument("--serve-requests", type=int, default=24,
-                    help="requests per serving run (the configured workload has 2000; 0 skips serving)")
-    ap.add_argument("--serve-requests-f64", type=int, default=None,
-                    help="requests for the plain FP64 server (default: the same stream)")
-    ap.add_argument("--serve-rates", type=float, nargs="*", default=[8.0],
-                    help="arrival rates (requests/s) for the batched mixed-precision server")
-    ap.add_argument("--serve-rates-f64", type=float, nargs="*", default=[3.0],
-                    help="arrival rates (requests/s) for the plain FP64 server")
+    ap.add_argument("--serve-requests", type=int, default=2000,
+                    help="requests per serving run (the configured workload: 2000; 0 skips serving)")
+    ap.add_argument("--serve-requests-f64", type=int, default=300,
+                    help="requests for the plain FP64 server (the first ones of the same stream)")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[16.0, 48.0],
+                    help="arrival rates (requests/s) for the batched mixed-precision server: one below "
+                         "saturation, one above it")
+    ap.add_argument("--serve-rates-f64", type=float, nargs="*", default=[12.0],
+                    help="arrival rates (requests/s) for the plain FP64 server (above its saturation)")
     ap.add_argument("--dims", type=int, nargs=4, default=list(DIMS),
                     help="lattice extents (default 32 32 32 64, the benchmark configuration)")
     args = ap.parse_args()

@@ -221,7 +221,9 @@ wd_status wd_check(wd_context *ctx, const wd_lattice *lat, const wd_field *b, co
 
 /* ---- host-buffer entry points (reference layout in and out) ------------ */
 /* Each uploads its inputs, runs on the device and downloads the result within
- * the call.  gauge is the reference's U.A[4]. */
+ * the call.  gauge is the reference's U.A[4].  After a return other than
+ * WD_OK the contents of dest are undefined (it may be partly written); no
+ * copy or kernel touches src or dest after the call returns. */
 wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
                               const double *src, double *dest, int dag, int cb);
 wd_status wd_host_dslash_full(wd_context *ctx, const int dims[4], const double *const gauge[4],
@@ -244,7 +246,9 @@ wd_status wd_host_cg(wd_context *ctx, const int dims[4], const double *const gau
  * device array that every GPU loading the library keeps until exit); larger n
  * returns WD_ERR_BAD_ARG.  The first call on a device looks up that array's
  * device address and should come before any stream capture.  All calls share
- * the array, so calls that overlap on the GPU race and give undefined results. */
+ * the array, so calls that overlap on the GPU race and give undefined results.
+ * The looked-up address is kept for the life of the process: resetting a
+ * device (cudaDeviceReset) after the first call on it is not supported. */
 wd_status wd_dot_noalloc(const double *a, const double *b, int64_t n, double *out, void *stream);
 
 /* ---- diagnostics (no counterpart in the reference) ---------------------- */

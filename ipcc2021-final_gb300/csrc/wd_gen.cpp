@@ -10,6 +10,11 @@
 //   N(0,1/2) real and imaginary off-diagonal parts, exponentiated by
 //   scaling-and-squaring Taylor series, then re-unitarised (Gram-Schmidt of
 //   rows 0 and 1, row 2 = conj(row0 x row1)) into SU(3).
+//
+// The CPU oracle compiles this same file, with the same flags, into its own
+// host-only library under the names wo_gen_gauge / wo_gen_source
+// (WD_GEN_ORACLE_NAMES), so that a CPU-only run of the reference's algorithm
+// draws bit-identical inputs without loading the CUDA library.
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -112,7 +117,15 @@ bool dims_ok(const int *dims, int64_t *V)
 
 }  // namespace
 
-extern "C" wd_status wd_gen_gauge(const int dims[4], uint64_t seed, double eps, double *const gauge[4])
+#ifdef WD_GEN_ORACLE_NAMES
+#define WD_GEN_GAUGE wo_gen_gauge
+#define WD_GEN_SOURCE wo_gen_source
+#else
+#define WD_GEN_GAUGE wd_gen_gauge
+#define WD_GEN_SOURCE wd_gen_source
+#endif
+
+extern "C" wd_status WD_GEN_GAUGE(const int dims[4], uint64_t seed, double eps, double *const gauge[4])
 {
     int64_t V;
     if (!dims_ok(dims, &V)) return WD_ERR_BAD_DIMS;
@@ -127,7 +140,7 @@ extern "C" wd_status wd_gen_gauge(const int dims[4], uint64_t seed, double eps, 
     return WD_OK;
 }
 
-extern "C" wd_status wd_gen_source(const int dims[4], uint64_t seed, double *src)
+extern "C" wd_status WD_GEN_SOURCE(const int dims[4], uint64_t seed, double *src)
 {
     int64_t V;
     if (!dims_ok(dims, &V)) return WD_ERR_BAD_DIMS;

@@ -15,7 +15,9 @@
 // use the array's name as a device address (on the host it is only a
 // stand-in symbol), so the first call on each device, with that device
 // current, looks the address up with cudaGetSymbolAddress and keeps it.
-// That first call should come before any stream capture.
+// That first call should come before any stream capture.  The address is
+// kept for the life of the process, so a device reset (cudaDeviceReset)
+// after the first call on that device is not supported.
 //
 // All calls share the one array: two calls whose kernels overlap on the GPU
 // (different streams, or different host threads without ordering) race on it

@@ -65,9 +65,30 @@ class Oracle:
         L.wo_cg_ref.argtypes = [vp, vp, d4, ip, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_double)]
         L.wo_cg_ref.restype = C.c_int
         L.wo_check.argtypes, L.wo_check.restype = [vp, vp, d4, ip, C.c_double, C.POINTER(C.c_double)], None
+        L.wo_cg_eo.argtypes = [vp, vp, d4, ip, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_double)]
+        L.wo_cg_eo.restype = C.c_int
+        L.wo_gen_gauge.argtypes, L.wo_gen_gauge.restype = [ip, C.c_uint64, C.c_double, d4], C.c_int
+        L.wo_gen_source.argtypes, L.wo_gen_source.restype = [ip, C.c_uint64, vp], C.c_int
 
     def threads(self, n: int = 0) -> int:
         return self.lib.wo_num_threads(n)
+
+    def gen_gauge(self, dims, seed: int, eps: float = 0.5) -> list[np.ndarray]:
+        """Seeded SU(3) links exp(i eps H) in the reference layout: the package's
+        generator (csrc/wd_gen.cpp) compiled into this library, so a CPU-only run
+        gets the GPU path's input bytes without loading the CUDA library."""
+        V = int(np.prod(dims))
+        gauge = [np.empty(V * 9, np.complex128) for _ in range(4)]
+        if self.lib.wo_gen_gauge(_d(dims), int(seed), float(eps), _g(gauge)) != 0:
+            raise ValueError(f"bad lattice extents {tuple(dims)}")
+        return gauge
+
+    def gen_source(self, dims, seed: int) -> np.ndarray:
+        """Seeded unit-norm Gaussian source (the package's generator)."""
+        src = np.empty(int(np.prod(dims)) * 12, np.complex128)
+        if self.lib.wo_gen_source(_d(dims), int(seed), _p(src)) != 0:
+            raise ValueError(f"bad lattice extents {tuple(dims)}")
+        return src
 
     def dslash_offd(self, src, gauge, dims, dag: bool, cb: int) -> np.ndarray:
         out = np.empty_like(src)
@@ -117,6 +138,17 @@ class Oracle:
         it = self.lib.wo_cg_ref(_p(src), _p(x), _g(gauge), _d(dims), float(mass), int(max_iter), float(accuracy),
                                 C.byref(rsd))
         return x, it, rsd.value
+
+    def cg_eo(self, src, gauge, dims, mass, tol: float = 1e-14, max_iter: int = 5000
+              ) -> tuple[np.ndarray, int, float]:
+        """Even-odd (Schur) CG from a zero guess until the normal residual is
+        tol relative; returns (solution, iterations, FP64 true residual
+        |b - Mx|/|b|).  Reference solutions at large volumes."""
+        x = np.empty_like(src)
+        res = C.c_double()
+        it = self.lib.wo_cg_eo(_p(src), _p(x), _g(gauge), _d(dims), float(mass), int(max_iter), float(tol),
+                               C.byref(res))
+        return x, it, res.value
 
     def check(self, b, x, gauge, dims, mass) -> np.ndarray:
         o = (C.c_double * 12)()

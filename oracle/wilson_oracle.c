@@ -73,8 +73,10 @@ static inline long eo_index(const int *L, int x, int y, int z, int t)
  * the half-spinor h = P psi(neighbour) is multiplied by W (U_mu(x) forward,
  * U_mu(x-mu)^dag backward), and t = W h feeds the four spin components.
  * The -1/2 is applied once at the end (the reference applies it per term).
+ * src holds sites from eo index src_off on (0: a full-lattice array; Vh: an
+ * array of the odd sites only).
  */
-static void hop_site(const cplx *src, const cplx *const U[4], const int *L, double flag,
+static void hop_site(const cplx *src, long src_off, const cplx *const U[4], const int *L, double flag,
                      int x, int y, int z, int t, cplx out[12])
 {
     int c[4] = {x, y, z, t};
@@ -86,7 +88,7 @@ static void hop_site(const cplx *src, const cplx *const U[4], const int *L, doub
             int n[4] = {c[0], c[1], c[2], c[3]};
             n[mu] = dir == 0 ? (c[mu] + 1) % L[mu] : (c[mu] - 1 + L[mu]) % L[mu];
             long nb = eo_index(L, n[0], n[1], n[2], n[3]);
-            const cplx *s = src + nb * 12;
+            const cplx *s = src + (nb - src_off) * 12;
             /* link: forward U_mu(x) at this site; backward U_mu(x-mu) at nb */
             const cplx *W = U[mu] + (dir == 0 ? here : nb) * 9;
             /* sign of the gamma term: (1 - g) forward, (1 + g) backward, times flag */
@@ -182,7 +184,7 @@ void wo_dslash_offd(const double *src_d, double *dest_d, const double *const gau
         for (int x = 0; x < L[0]; ++x) {
             if (((x + y + z + t) & 1) != cb)
                 continue;
-            hop_site(src, U, L, flag, x, y, z, t, dest + eo_index(L, x, y, z, t) * 12);
+            hop_site(src, 0, U, L, flag, x, y, z, t, dest + eo_index(L, x, y, z, t) * 12);
         }
     }
 }
@@ -219,7 +221,7 @@ void wo_dslash_full(const double *src_d, double *dest_d, const double *const gau
         for (int x = 0; x < L[0]; ++x) {
             long e = eo_index(L, x, y, z, t);
             cplx h[12];
-            hop_site(src, U, L, flag, x, y, z, t, h);
+            hop_site(src, 0, U, L, flag, x, y, z, t, h);
             for (int k = 0; k < 12; ++k)
                 dest[e * 12 + k] = c_add(c_scale(src[e * 12 + k], a), h[k]);
         }
@@ -336,6 +338,131 @@ int wo_cg_ref(const double *src, double *dest, const double *const gauge[4], con
     if (rsd_out)
         *rsd_out = rsd;
     return iters;
+}
+
+/*
+ * One parity of the hopping term on half-lattice arrays: out[i] (the site of
+ * parity cb with eo index cb*Vh + i) = -1/2 sum_mu hop(in), where in[j] is the
+ * site of parity 1-cb with eo index (1-cb)*Vh + j.  This is the interior of
+ * DslashoffdNew (src/dslash_new.cpp:1341-2677) without its memset of the
+ * other parity.  flag -1 gives the hopping term of M^dag.
+ */
+static void hop_half(const cplx *in, cplx *out, const cplx *const U[4], const int *L, double flag, int cb)
+{
+    long vh = (long)L[0] * L[1] * L[2] * L[3] / 2;
+    long rows = (long)L[1] * L[2] * L[3];
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < rows; ++r) {
+        int y = (int)(r % L[1]);
+        int z = (int)((r / L[1]) % L[2]);
+        int t = (int)(r / ((long)L[1] * L[2]));
+        for (int x = 0; x < L[0]; ++x) {
+            if (((x + y + z + t) & 1) != cb)
+                continue;
+            hop_site(in, (1 - cb) * vh, U, L, flag, x, y, z, t, out + (eo_index(L, x, y, z, t) - cb * vh) * 12);
+        }
+    }
+}
+
+/*
+ * Schur complement on the even sites: out = a*in - H_eo H_oe in / a, with
+ * H = -1/2 D the hopping term (M = a + H, a = 4 + m).  flag -1 gives the
+ * adjoint, a - (H^dag)_eo (H^dag)_oe / a.  tmp: Vh*12 entries.
+ */
+static void schur_apply(const cplx *in, cplx *out, cplx *tmp, const cplx *const U[4], const int *L, double a,
+                        double flag)
+{
+    long n = (long)L[0] * L[1] * L[2] * L[3] / 2 * 12;
+    hop_half(in, tmp, U, L, flag, 1);
+    hop_half(tmp, out, U, L, flag, 0);
+    double ia = 1.0 / a;
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) {
+        out[i].re = a * in[i].re - ia * out[i].re;
+        out[i].im = a * in[i].im - ia * out[i].im;
+    }
+}
+
+/*
+ * Even-odd (Schur) preconditioned CG -- the solver form of the IPCC 2021
+ * problem statement (doc/IPCC_2021.pdf, p.9-11), used here to produce
+ * reference solutions cheaply at large volumes; CGinvert (src/invert.cpp:25-121,
+ * wo_cg_ref above) solves the same M x = b on the full lattice.
+ *   b^_e = b_e - H_eo b_o / a;  CG on  M^dag M^ x_e = M^dag b^_e  (real alpha,
+ *   beta) until |r| <= tol |M^dag b^_e|;  x_o = (b_o - H_oe x_e) / a.
+ * dest receives the full-lattice solution (reference layout, even sites
+ * first).  *true_res_out = |b - M x| / |b| recomputed with the full operator.
+ * Returns the iteration count (max when it did not converge).
+ */
+int wo_cg_eo(const double *src_d, double *dest_d, const double *const gauge_d[4], const int *L, double mass,
+             int max, double tol, double *true_res_out)
+{
+    const cplx *src = (const cplx *)src_d;
+    cplx *dest = (cplx *)dest_d;
+    const cplx *U[4] = {(const cplx *)gauge_d[0], (const cplx *)gauge_d[1],
+                        (const cplx *)gauge_d[2], (const cplx *)gauge_d[3]};
+    long V = (long)L[0] * L[1] * L[2] * L[3], vh = V / 2, n = vh * 12;
+    double a = 4.0 + mass;
+    size_t bytes = sizeof(cplx) * (size_t)n;
+    cplx *bh = (cplx *)malloc(bytes), *r = (cplx *)malloc(bytes), *p = (cplx *)malloc(bytes);
+    cplx *q = (cplx *)malloc(bytes), *q2 = (cplx *)malloc(bytes), *tmp = (cplx *)malloc(bytes);
+    cplx *x = dest; /* even half of dest */
+    const cplx *b_e = src, *b_o = src + n;
+    int it = 0;
+
+    hop_half(b_o, tmp, U, L, 1.0, 0);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) {
+        bh[i].re = b_e[i].re - tmp[i].re / a;
+        bh[i].im = b_e[i].im - tmp[i].im / a;
+    }
+    schur_apply(bh, r, tmp, U, L, a, -1.0);
+    memset(x, 0, bytes);
+    memcpy(p, r, bytes);
+    double rr = wo_norm2((const double *)r, n);
+    const double stop = tol * tol * rr;
+    while (it < max && rr > stop) {
+        schur_apply(p, q, tmp, U, L, a, 1.0);
+        schur_apply(q, q2, tmp, U, L, a, -1.0);
+        double alpha = rr / wo_norm2((const double *)q, n);
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < n; ++i) {
+            x[i].re += alpha * p[i].re;
+            x[i].im += alpha * p[i].im;
+            r[i].re -= alpha * q2[i].re;
+            r[i].im -= alpha * q2[i].im;
+        }
+        double rr_new = wo_norm2((const double *)r, n);
+        double beta = rr_new / rr;
+        rr = rr_new;
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < n; ++i) {
+            p[i].re = r[i].re + beta * p[i].re;
+            p[i].im = r[i].im + beta * p[i].im;
+        }
+        ++it;
+    }
+    /* x_o = (b_o - H_oe x_e) / a */
+    hop_half(x, tmp, U, L, 1.0, 1);
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < n; ++i) {
+        dest[n + i].re = (b_o[i].re - tmp[i].re) / a;
+        dest[n + i].im = (b_o[i].im - tmp[i].im) / a;
+    }
+    if (true_res_out) {
+        cplx *full = (cplx *)malloc(2 * bytes);
+        wo_dslash_full(dest_d, (double *)full, gauge_d, L, mass, 0);
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < 2 * n; ++i) {
+            full[i].re = src[i].re - full[i].re;
+            full[i].im = src[i].im - full[i].im;
+        }
+        double nb = wo_norm2(src_d, 2 * n);
+        *true_res_out = sqrt(wo_norm2((const double *)full, 2 * n) / (nb > 0 ? nb : 1.0));
+        free(full);
+    }
+    free(bh); free(r); free(p); free(q); free(q2); free(tmp);
+    return it;
 }
 
 /*

@@ -4,7 +4,9 @@
 //   compat_golden in.bin out.bin
 // in.bin:  int32 dims[4], float64 mass, int32 cg_seed, gauge 4*V*9 complex, src V*12 complex
 // out.bin: for each named output, V*12 complex, in the order written below;
-//          then float64 norm_2(src), complex vector_p(src, DslashNew(src)), int32 CG iterations
+//          then float64 norm_2(src), complex vector_p(src, DslashNew(src)), the CGinvert
+//          solution of the object overload, then that of the raw-pointer overload
+//          (src/invert.cpp:15-23) on plain arrays, both after srand(cg_seed)
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
@@ -67,6 +69,12 @@ int main(int argc, char **argv)
     lattice_fermion x(subgs, dims);
     CGinvert(src, x, U, mass, 500, 1e-9);
     put(x);
+    // the raw-pointer overload, as a caller holding plain arrays uses it
+    std::vector<cd> raw_src(s), raw_x(V * 12);
+    int subgs2[4] = {dims[0], dims[1], dims[2], dims[3]}, site_vec2[4] = {dims[0], dims[1], dims[2], dims[3]};
+    std::srand(seed);
+    CGinvert(raw_src.data(), raw_x.data(), gp, mass, 500, 1e-9, subgs2, site_vec2);
+    std::fwrite(raw_x.data(), 16, raw_x.size(), o);
     std::fclose(o);
     return 0;
 }

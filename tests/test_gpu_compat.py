@@ -53,6 +53,7 @@ def test_reference_api_on_golden_vectors(wd, oracle, golden4, golden_prog, tmp_p
     norm2 = tail[:8].view(np.float64)[0]
     dot = tail[8:24].view(np.complex128)[0]
     x = tail[24:24 + n].view(np.complex128)
+    x_ptr = tail[24 + n:24 + 2 * n].view(np.complex128)
     names = ["offd_new_dag0_cb0", "offd_new_dag0_cb1", "offd_new_dag1_cb0", "offd_new_dag1_cb1",
              "full_new_dag0", "full_new_dag1", "full_old_dag0", "eeoo_new", "offd_new_dag0_cb0",
              "offd_new_dag1_cb1"]
@@ -67,10 +68,15 @@ def test_reference_api_on_golden_vectors(wd, oracle, golden4, golden_prog, tmp_p
     assert abs(norm2 - np.vdot(g["src"], g["src"]).real) < 1e-14
     ref_dot = np.vdot(g["src"], g["full_new_dag0"])
     assert abs(dot - ref_dot) < 1e-13 * abs(ref_dot)
-    # CGinvert with srand(cg_seed): the reference's own run gave cg_iters / cg_x
-    m = re.search(r"CG: (\d+) iterations, convergence residual \|r\| = ([0-9.eE+-]+)", r.stdout)
-    assert m and int(m.group(1)) == int(g["cg_iters"]), r.stdout
+    # CGinvert with srand(cg_seed), object overload then raw-pointer overload:
+    # the reference's own run gave cg_iters / cg_x
+    runs = re.findall(r"CG: (\d+) iterations, convergence residual \|r\| = ([0-9.eE+-]+)", r.stdout)
+    assert len(runs) == 2, r.stdout
+    for its, _ in runs:
+        assert int(its) == int(g["cg_iters"]), r.stdout
     assert rel_l2(x, g["cg_x"]) < 1e-10
+    assert rel_l2(x_ptr, g["cg_x"]) < 1e-10
+    assert np.array_equal(x_ptr, x)
 
 
 def test_command_line_driver_matches_oracle(wd, oracle):

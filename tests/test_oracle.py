@@ -143,3 +143,42 @@ def test_oracle_matches_reference_digests_8c16(oracle, digest8):
     assert iters == int(d["cg_iters"])
     assert abs(rsd - float(d["cg_rsd"])) < 1e-6 * float(d["cg_rsd"])
     assert digest_error(d, "cg_x", x) < 1e-11
+
+
+@pytest.mark.parametrize("which", ["golden4", "golden6"])
+def test_schur_cg_agrees_with_cginvert(oracle, which, request):
+    """The even-odd (Schur) CG that supplies reference solutions at large
+    volumes solves the same M x = b as the reference's CGinvert: both driven
+    to 1e-13 agree to 1e-12, and its recomputed true residual is tiny."""
+    g = request.getfixturevalue(which)
+    for mass in (g["mass"], 0.01):
+        xe, it, res = oracle.cg_eo(g["src"], g["gauge"], g["dims"], mass, tol=1e-14)
+        assert 0 < it < 5000 and res < 1e-12
+        b = g["src"]
+        r = b - oracle.dslash_full(xe, g["gauge"], g["dims"], mass, 0)
+        assert np.linalg.norm(r) / np.linalg.norm(b) == pytest.approx(res, rel=1e-6, abs=1e-16)
+        xr, _, _ = oracle.cg_ref(b, g["gauge"], g["dims"], mass, 5000, 1e-13 * np.linalg.norm(b),
+                                 np.zeros_like(b))
+        assert rel_l2(xe, xr) < 1e-12
+
+
+def test_schur_cg_matches_reference_cginvert_solutions(oracle, golden4, digest8):
+    """Against the reference's own CGinvert solutions: the 4^4 golden run
+    (normal residual 1e-9) and the 8^3x16 digest (1e-10)."""
+    from conftest import digest_error
+    g = golden4
+    xe, _, _ = oracle.cg_eo(g["src"], g["gauge"], g["dims"], g["mass"])
+    assert rel_l2(g["cg_x"], xe) < 1e-8
+    d = digest8
+    xe, _, _ = oracle.cg_eo(d["src"], d["gauge"], d["dims"], d["mass"])
+    assert digest_error(d, "cg_x", xe) < 1e-9
+
+
+@pytest.mark.parametrize("dims,seed", [((8, 8, 8, 16), 1), ((6, 4, 2, 4), 3), ((4, 4, 4, 8), 2**62 + 5)])
+def test_oracle_generator_bytes_equal_package_generator(wd, oracle, dims, seed):
+    """The oracle library carries the package's input generator, so a
+    CPU-only run (the reference arm of the benchmark) gets the same bytes
+    without loading the CUDA library."""
+    for a, b in zip(wd.gen_gauge(dims, seed, 0.5), oracle.gen_gauge(dims, seed, 0.5)):
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    assert np.array_equal(wd.gen_source(dims, seed).view(np.uint64), oracle.gen_source(dims, seed).view(np.uint64))

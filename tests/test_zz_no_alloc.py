@@ -22,24 +22,43 @@ def noalloc(wd):
     return f
 
 
-def test_dot_noalloc_matches_dot_on_two_calls(wd, ctx):
+def _call(wd, f, a, b):
     import torch
 
+    da = torch.from_numpy(a).to("cuda")
+    db = torch.from_numpy(b).to("cuda")
+    out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+    st = f(da.data_ptr(), db.data_ptr(), a.size, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == wd.OK
+    torch.cuda.synchronize()
+    return complex(*out.cpu().numpy())
+
+
+def test_dot_noalloc_matches_dot_on_two_calls(wd, ctx):
+    """Lattice fields of 3 chunks, then 1 chunk, then 3 chunks again: each
+    call against wd_dot on the same data."""
     f = noalloc(wd)
-    stream = torch.cuda.current_stream()
-    for dims, seed in (((8, 4, 4, 8), 11), ((4, 4, 2, 4), 12)):
+    for dims, seed in (((8, 4, 4, 8), 11), ((4, 4, 2, 4), 12), ((8, 4, 4, 8), 13)):
         a = wd.gen_source(dims, seed)
         b = wd.gen_source(dims, seed + 100) + 0.5j * a
         lat = ctx.lattice(dims, wd.gen_gauge(dims, seed))
         expected = lat.field(a).dot(lat.field(b))          # existing entry point
-        da = torch.from_numpy(a).to("cuda")
-        db = torch.from_numpy(b).to("cuda")
-        out = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
-        st = f(da.data_ptr(), db.data_ptr(), a.size, out.data_ptr(), stream.cuda_stream)
-        assert st == wd.OK
-        torch.cuda.synchronize()
-        got = complex(*out.cpu().numpy())
+        got = _call(wd, f, a, b)
         assert abs(got - expected) <= TOL * abs(expected), (got, expected)
+
+
+def test_dot_noalloc_partial_last_chunk(wd, ctx):
+    """A small call, then n = 2*4096 + 17 (three chunks, the last one partial)
+    from flat arrays, against numpy: a wrong chunk count or stale partial sums
+    from the earlier calls would show."""
+    f = noalloc(wd)
+    rng = np.random.default_rng(21)
+    for n in (100, 2 * 4096 + 17):
+        a = rng.normal(size=n) + 1j * rng.normal(size=n)
+        b = rng.normal(size=n) + 1j * rng.normal(size=n)
+        expected = np.vdot(a, b)
+        got = _call(wd, f, a, b)
+        assert abs(got - expected) <= TOL * abs(expected), (n, got, expected)
 
 
 def test_dot_noalloc_limits(wd, ctx):
