@@ -72,6 +72,7 @@ extern "C" wd_status wd_context_create(int device, wd_context **out)
     if (e == cudaSuccess)
         e = cudaMalloc(&ctx->red_partial, sizeof(double2) * (WD_RED_BLOCKS + WD_RED_SLOTS));
     if (e == cudaSuccess) e = cudaHostAlloc(&ctx->red_result, sizeof(double2) * WD_RED_SLOTS, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&ctx->state_host, WD_STATE_HOST_BYTES, 0);
     if (e != cudaSuccess) {
         wd_context_destroy(ctx);
         cudaGetLastError();
@@ -147,6 +148,7 @@ extern "C" void wd_context_destroy(wd_context *ctx)
     cudaFree(ctx->red_partial);
     cudaFree(ctx->staging);
     if (ctx->red_result) cudaFreeHost(ctx->red_result);
+    if (ctx->state_host) cudaFreeHost(ctx->state_host);
     for (auto &ev : ctx->chunk_done)
         if (ev) cudaEventDestroy(ev);
     for (auto &ev : ctx->chunk_in)

@@ -10,6 +10,8 @@
 #include "wd_hop.cuh"
 #include "wd_lp_staged.cuh"
 #include "wd_kernels.h"
+#include "wd_reduce.cuh"
+#include "wd_solver.h"
 #include <type_traits>
 #include "wd_tune.h"
 
@@ -28,6 +30,7 @@ struct HopLP {
     Lk link;
     bool has_x;
     float alpha, beta;
+    const int *stop = nullptr;  // gate: no-op launch while *stop != 0 (device-driven solver loops)
 
     __device__ __forceinline__ void load_in(int s, C *v) const { in.load(s, v); }
     __device__ __forceinline__ float load_in_raw(int s, C *v) const
@@ -165,6 +168,7 @@ __global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_lp
     using Sp = decltype(p.in);
     using Lk = decltype(p.link);
     __shared__ LpStage<Sp, Lk, P::kThreads> st;
+    if (wd_gate_closed(p)) return;
     const int s = blockIdx.x * P::kThreads + threadIdx.x;
     if (s >= p.g.Vh) return;
     float2 acc[12];
@@ -201,7 +205,7 @@ wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p
         auto make = [&](auto threads, auto minb) {
             HopLP<Sp, Lk, decltype(threads)::value, decltype(minb)::value> q;
             q.g = p.g, q.cb = p.cb, q.in = p.in, q.out = p.out, q.x = p.x, q.link = p.link;
-            q.has_x = p.has_x, q.alpha = p.alpha, q.beta = p.beta;
+            q.has_x = p.has_x, q.alpha = p.alpha, q.beta = p.beta, q.stop = p.stop;
             return q;
         };
         using I0 = std::integral_constant<int, 0>;
@@ -242,7 +246,7 @@ wd_status wd_lattice_gauge_lp(wd_context *ctx, const wd_lattice *lat_c, wd_preci
 }
 
 wd_status wd_hop_f32(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
-                     double alpha, double beta)
+                     double alpha, double beta, const int *stop)
 {
     wd_status st = wd_lattice_gauge_lp(ctx, lat, WD_PREC_F32);
     if (st != WD_OK) return st;
@@ -256,11 +260,12 @@ wd_status wd_hop_f32(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out
     p.link = LinkF32{(const float4 *)lat->gauge_f32, lat->g.Vh};
     p.alpha = (float)alpha;
     p.beta = (float)beta;
+    p.stop = stop;
     return launch_tuned(ctx, "hop_f32", p, dag);
 }
 
 wd_status wd_hop_f16(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
-                     double alpha, double beta)
+                     double alpha, double beta, const int *stop)
 {
     wd_status st = wd_lattice_gauge_lp(ctx, lat, WD_PREC_F16);
     if (st != WD_OK) return st;
@@ -275,6 +280,7 @@ wd_status wd_hop_f16(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out
     p.link = LinkF16{a, (const uint2 *)(a + (size_t)8 * lat->g.Vh), lat->g.Vh};
     p.alpha = (float)alpha;
     p.beta = (float)beta;
+    p.stop = stop;
     return launch_tuned(ctx, "hop_f16", p, dag);
 }
 
@@ -312,4 +318,235 @@ wd_status wd_spinor_h16_to_ref(wd_context *ctx, const WdGeom &g, WdVec f, double
         WD_LAUNCHED(ctx);
     }
     return WD_OK;
+}
+
+// ===================================================================
+// Reducing operator steps of the mixed-precision CG (wd_mixed.cu): the
+// second hop of t = Mhat p also reduces |t|^2, the second hop of
+// q = Mhat^dag t applies the CG update instead of storing q.  One block
+// partial per block; the last block to finish (a one-shot atomic counter, no
+// waiting) folds the partials in a fixed order -- the result does not depend
+// on which block finishes last -- and updates the solver's device scalars.
+namespace {
+
+enum { kEpiNorm = 0, kEpiUpdate = 1 };
+
+template <class Sp, class Lk, int THREADS, int MINB, int EPI>
+struct HopLPRed : HopLP<Sp, Lk, THREADS, MINB> {
+    WdMxDev *dev;
+    double *partial;
+    Sp pvec;       // update: p at the output site (x_s += alpha p)
+    SpF32 rs, xs;  // update: iterated residual and solution increment
+
+    // out = alpha acc + beta x, then the site's contribution to the reduction
+    __device__ __forceinline__ float epilogue_red(int s, const float2 *acc) const
+    {
+        float2 r[12], xv[12];
+        float bx = this->beta;  // beta times the x site's scale
+        if constexpr (Sp::kScaled) bx *= this->x.load_raw(s, xv);
+        else this->x.load(s, xv);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) r[c] = c_axpby(this->alpha, acc[c], bx, xv[c]);
+        float n = 0.f;
+        if constexpr (EPI == kEpiNorm) {
+#pragma unroll
+            for (int c = 0; c < 12; ++c) n = fmaf(r[c].x, r[c].x, fmaf(r[c].y, r[c].y, n));
+            this->out.store(s, r);
+        } else {
+            const float a = dev->alpha;
+            rs.load(s, xv);
+#pragma unroll
+            for (int c = 0; c < 12; ++c) {
+                xv[c] = make_float2(fmaf(-a, r[c].x, xv[c].x), fmaf(-a, r[c].y, xv[c].y));
+                n = fmaf(xv[c].x, xv[c].x, fmaf(xv[c].y, xv[c].y, n));
+            }
+            rs.store(s, xv);
+            pvec.load(s, r);
+            xs.load(s, xv);
+#pragma unroll
+            for (int c = 0; c < 12; ++c) xv[c] = make_float2(fmaf(a, r[c].x, xv[c].x), fmaf(a, r[c].y, xv[c].y));
+            xs.store(s, xv);
+        }
+        return n;
+    }
+};
+
+// t reduced: alpha = rr / |t|^2
+__device__ __forceinline__ void mx_fin_norm(WdMxDev *d, double tt)
+{
+    d->tt = tt;
+    if (!(tt > 0.0) || !isfinite(tt)) {
+        d->stop = 2;
+        return;
+    }
+    d->alpha = (float)(d->rr / tt);
+}
+
+// |r_s|^2 after the update: the reliable-update rule of wd_mixed.cu
+__device__ __forceinline__ void mx_fin_update(WdMxDev *d, double rr_new)
+{
+    d->rr_new = rr_new;
+    d->iters += 1;
+    if (!isfinite(rr_new)) {
+        d->stop = 2;
+        return;
+    }
+    if (rr_new < d->delta2 * d->rr_max || rr_new <= d->target2) {
+        d->stop = 1;  // the host runs the update; rr keeps the previous iterate's value
+        return;
+    }
+    d->beta = (float)(rr_new / d->rr);
+    d->rr = rr_new;
+}
+
+template <bool DAG, bool STAGED, int EPI, class P>
+__device__ __forceinline__ float red_site(const P &p, int s)
+{
+    float v = 0.f;
+    if constexpr (STAGED) {
+        using Sp = decltype(p.in);
+        using Lk = decltype(p.link);
+        __shared__ LpStage<Sp, Lk, P::kThreads> st;
+        if (s < p.g.Vh) {
+            float2 acc[12];
+            lp_hop_site_staged<DAG>(p, s, acc, st);
+            v = p.epilogue_red(s, acc);
+        }
+    } else {
+        if (s < p.g.Vh) {
+            float2 acc[12];
+            wd_hop_site<DAG>(p, s, acc);
+            v = p.epilogue_red(s, acc);
+        }
+    }
+    return v;
+}
+
+template <bool DAG, bool STAGED, int EPI, class P>
+__global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_lp_red(const P p)
+{
+    constexpr int T = P::kThreads;
+    if (p.dev->stop) return;  // the same value in every block of the launch
+    const int s = blockIdx.x * T + threadIdx.x;
+    const double v = wd_warp_sum((double)red_site<DAG, STAGED, EPI>(p, s));
+    __shared__ double sw[T / 32];
+    __shared__ int last;
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sw[w] = v;
+    __syncthreads();
+    unsigned *counter = EPI == kEpiNorm ? &p.dev->count_t : &p.dev->count_r;
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+#pragma unroll
+        for (int i = 0; i < T / 32; ++i) b += sw[i];
+        p.partial[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double t = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += T) t += __ldcg(p.partial + i);
+    t = wd_warp_sum(t);
+    __syncthreads();
+    if (l == 0) sw[w] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double tot = 0.0;
+#pragma unroll
+        for (int i = 0; i < T / 32; ++i) tot += sw[i];
+        *counter = 0;
+        if constexpr (EPI == kEpiNorm) mx_fin_norm(p.dev, tot);
+        else mx_fin_update(p.dev, tot);
+    }
+}
+
+// the launch shape the tuner chose for the plain hop of this storage and size
+template <int EPI, class Sp, class Lk>
+wd_status launch_red(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &b, int dag, WdMxDev *dev,
+                     double *partial, Sp pvec, SpF32 rs, SpF32 xs)
+{
+    constexpr bool kF16 = std::is_same_v<Sp, SpF16>;
+    int v = wd_tune_choice(ctx, name, b.g.Vh);
+    if (v < 0 || v == 3) v = 0;  // 3 caps registers at 64: the reducing epilogues would spill
+    auto run = [&](auto threads, auto minb, auto staged) -> wd_status {
+        constexpr int TH = decltype(threads)::value, MB = decltype(minb)::value;
+        constexpr bool ST = decltype(staged)::value;
+        HopLPRed<Sp, Lk, TH, MB, EPI> q;
+        q.g = b.g, q.cb = b.cb, q.in = b.in, q.out = b.out, q.x = b.x, q.link = b.link;
+        q.has_x = true, q.alpha = b.alpha, q.beta = b.beta;
+        q.dev = dev, q.partial = partial, q.pvec = pvec, q.rs = rs, q.xs = xs;
+        const int blocks = (b.g.Vh + TH - 1) / TH;
+        if (dag) k_hop_lp_red<true, ST, EPI><<<blocks, TH, 0, ctx->stream>>>(q);
+        else k_hop_lp_red<false, ST, EPI><<<blocks, TH, 0, ctx->stream>>>(q);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
+    using I0 = std::integral_constant<int, 0>;
+    using T64 = std::integral_constant<int, 64>;
+    using T128 = std::integral_constant<int, 128>;
+    using Yes = std::true_type;
+    using No = std::false_type;
+    if constexpr (kF16) {
+        if (v == 4) return run(T128(), std::integral_constant<int, 6>(), Yes());
+        if (v == 5) return run(T64(), std::integral_constant<int, 12>(), Yes());
+    }
+    switch (v) {
+    case 1: return run(T64(), I0(), No());
+    case 2: return run(std::integral_constant<int, 256>(), I0(), No());
+    default: return run(T128(), I0(), No());
+    }
+}
+
+template <class Sp, class Lk>
+HopLP<Sp, Lk> red_base(const wd_lattice *lat, Sp in, Sp out, Sp x, Lk link, double mass)
+{
+    const double a = 4.0 + mass;
+    HopLP<Sp, Lk> b;
+    b.g = lat->g;
+    b.cb = 0;
+    b.in = in, b.out = out, b.x = x, b.link = link;
+    b.has_x = true;
+    b.alpha = (float)(-0.25 / a);
+    b.beta = (float)a;
+    return b;
+}
+
+template <int EPI>
+wd_status hop_lp_red(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, WdVec x, WdVec p, WdVec rs,
+                     WdVec xs, double mass, int dag, WdMxDev *dev, double *partial)
+{
+    const int Vh = lat->g.Vh;
+    if (in.prec != x.prec || in.prec != p.prec || (in.prec != WD_PREC_F32 && in.prec != WD_PREC_F16))
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "reducing hop: FP32 or FP16 operands of one storage");
+    wd_status st = wd_lattice_gauge_lp(ctx, lat, in.prec);
+    if (st != WD_OK) return st;
+    const SpF32 r32 = sp_f32(rs, Vh), x32 = sp_f32(xs, Vh);
+    if (in.prec == WD_PREC_F32) {
+        const LinkF32 lk{(const float4 *)lat->gauge_f32, Vh};
+        return launch_red<EPI>(ctx, "hop_f32", red_base(lat, sp_f32(in, Vh), sp_f32(out, Vh), sp_f32(x, Vh), lk, mass),
+                               dag, dev, partial, sp_f32(p, Vh), r32, x32);
+    }
+    const uint4 *a = (const uint4 *)lat->gauge_h12;
+    const LinkF16 lk{a, (const uint2 *)(a + (size_t)8 * Vh), Vh};
+    return launch_red<EPI>(ctx, "hop_f16", red_base(lat, sp_f16(in, Vh), sp_f16(out, Vh), sp_f16(x, Vh), lk, mass), dag,
+                           dev, partial, sp_f16(p, Vh), r32, x32);
+}
+
+}  // namespace
+
+wd_status wd_hop_lp_norm(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec t, WdVec p, double mass,
+                         WdMxDev *dev, double *partial)
+{
+    WdVec none;
+    none.prec = WD_PREC_F32;
+    return hop_lp_red<kEpiNorm>(ctx, lat, in, t, p, p, none, none, mass, 0, dev, partial);
+}
+
+wd_status wd_hop_lp_update(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec t, WdVec p, WdVec rs, WdVec xs,
+                           double mass, WdMxDev *dev, double *partial)
+{
+    // out is not written by the update epilogue
+    return hop_lp_red<kEpiUpdate>(ctx, lat, in, t, t, p, rs, xs, mass, 1, dev, partial);
 }

@@ -322,9 +322,24 @@ struct wd_min_blocks : std::integral_constant<int, 0> {};
 template <class P>
 struct wd_min_blocks<P, std::void_t<decltype(P::kMinBlocks)>> : std::integral_constant<int, P::kMinBlocks> {};
 
+// Optional gate: a policy with a member `const int *stop` (non-null) makes the
+// launch a no-op while *stop != 0 (device-driven solver loops queue
+// iterations ahead and close the gate from the device).
+template <class P, class = void>
+struct wd_has_gate : std::false_type {};
+template <class P>
+struct wd_has_gate<P, std::void_t<decltype(P::stop)>> : std::true_type {};
+template <class P>
+__device__ __forceinline__ bool wd_gate_closed(const P &p)
+{
+    if constexpr (wd_has_gate<P>::value) return p.stop && *p.stop;
+    return false;
+}
+
 template <bool DAG, class P>
 __global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) wd_hop_kernel(const P p)
 {
+    if (wd_gate_closed(p)) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= p.g.Vh) return;
     typename P::C acc[12];

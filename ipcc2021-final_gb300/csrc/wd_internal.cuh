@@ -19,6 +19,9 @@
 
 #define WD_MAX_SITES (int64_t(1) << 30)
 
+// pinned host bytes for reading back a solver's device-side scalars
+constexpr size_t WD_STATE_HOST_BYTES = 4096;
+
 // compute chunks and upload units of the pipelined host-buffer hopping term
 constexpr int WD_MAX_CHUNKS = 16;
 constexpr int WD_MAX_UPLOADS = 32;
@@ -44,6 +47,7 @@ struct wd_context {
     // used for layout conversion of host buffers.
     void *red_partial = nullptr;  // WD_RED_BLOCKS double2 (+ result slots)
     void *red_result = nullptr;   // pinned host mirror of the reduction results
+    void *state_host = nullptr;   // pinned host mirror of a solver's device scalars (WD_STATE_HOST_BYTES)
     void *staging = nullptr;      // device staging buffer for reference-layout copies
     size_t staging_bytes = 0;
     // cached host-buffer path state (wd_host_*): one lattice + fields

@@ -64,10 +64,24 @@ wd_status wd_v_zero(wd_context *ctx, WdVec v, int64_t n);
 
 // ---- FP32 / FP16 storage (wd_lp.cuh) with 12-real links
 wd_status wd_lattice_gauge_lp(wd_context *ctx, const wd_lattice *lat, wd_precision prec);
+// stop (device, optional): the launch is a no-op while *stop != 0
 wd_status wd_hop_f32(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
-                     double alpha, double beta);
+                     double alpha, double beta, const int *stop = nullptr);
 wd_status wd_hop_f16(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, const WdVec *x, int cb, int dag,
-                     double alpha, double beta);
+                     double alpha, double beta, const int *stop = nullptr);
+struct WdMxDev;
+// The two reducing operator steps of a mixed-precision CG iteration on even
+// blocks (FP32 or FP16 storage, 12-real links), with the device scalars dev:
+//  * norm:   t = -D_eo in / (4a) + a p  (in = D_oe p, odd), stored; |t|^2 is
+//            reduced and dev->alpha = rr / |t|^2 set by the last block;
+//  * update: q = -D_eo^dag in / (4a) + a t (in = D_oe^dag t), not stored:
+//            rs -= alpha q, xs += alpha p, and |rs|^2 reduced; the last block
+//            applies the reliable-update rule (wd_solver.h).
+// partial: at least Vh/64 + 1 doubles.  Both are no-ops while dev->stop != 0.
+wd_status wd_hop_lp_norm(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec t, WdVec p, double mass,
+                         WdMxDev *dev, double *partial);
+wd_status wd_hop_lp_update(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec t, WdVec p, WdVec rs, WdVec xs,
+                           double mass, WdMxDev *dev, double *partial);
 // FP64 block [12][Vh] <-> low-precision block; accumulate != 0 adds into out
 wd_status wd_lp_from_f64(wd_context *ctx, int Vh, const double2 *in, WdVec out);
 wd_status wd_lp_to_f64(wd_context *ctx, int Vh, WdVec in, double2 *out, int accumulate);

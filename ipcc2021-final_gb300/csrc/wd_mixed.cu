@@ -12,6 +12,7 @@
 //   x_e += x_s;  s = bhat - Mhat x_e;  r_s = Mhat^dag s (FP32);  x_s <- 0
 // |s| is the true residual |b - M x| of the full system, so convergence is
 // decided on the recomputed high-precision residual, never on the iterated one.
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include "wd_df.cuh"
@@ -66,35 +67,28 @@ __device__ __forceinline__ dfr df_sq_acc(dfr acc, float2 v)
 
 #define SITE_STRIDE(s, Vh) for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < (Vh); s += gridDim.x * blockDim.x)
 
-// x_s += alpha p; r_s -= alpha q; partial |r_s|^2
-template <class SpL>
-__global__ void __launch_bounds__(WD_RED_THREADS) k_mx_update(float alpha, SpL p, SpL q, SpF32 xs, SpF32 rs, int Vh,
-                                                              double2 *partial)
-{
-    dfr acc{0.f, 0.f};
-    SITE_STRIDE(s, Vh)
-    {
-        float2 pv[12], qv[12], xv[12], rv[12];
-        p.load(s, pv);
-        q.load(s, qv);
-        xs.load(s, xv);
-        rs.load(s, rv);
-#pragma unroll
-        for (int c = 0; c < 12; ++c) {
-            xv[c] = make_float2(fmaf(alpha, pv[c].x, xv[c].x), fmaf(alpha, pv[c].y, xv[c].y));
-            rv[c] = make_float2(fmaf(-alpha, qv[c].x, rv[c].x), fmaf(-alpha, qv[c].y, rv[c].y));
-            acc = df_sq_acc(acc, rv[c]);
-        }
-        xs.store(s, xv);
-        rs.store(s, rv);
-    }
-    wd_block_partial(df_value(acc), 0.0, partial);
-}
-
 // p = r_s + beta p
 template <class SpL>
 __global__ void k_mx_xpay(SpF32 rs, float beta, SpL p, int Vh)
 {
+    SITE_STRIDE(s, Vh)
+    {
+        float2 rv[12], pv[12];
+        rs.load(s, rv);
+        p.load(s, pv);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) pv[c] = make_float2(fmaf(beta, pv[c].x, rv[c].x), fmaf(beta, pv[c].y, rv[c].y));
+        p.store(s, pv);
+    }
+}
+
+// p = r_s + beta p with beta from the device scalars; a no-op while a
+// reliable update is due (d->stop != 0)
+template <class SpL>
+__global__ void k_mx_xpay_dev(SpF32 rs, const WdMxDev *d, SpL p, int Vh)
+{
+    if (d->stop) return;
+    const float beta = d->beta;
     SITE_STRIDE(s, Vh)
     {
         float2 rv[12], pv[12];
@@ -186,18 +180,6 @@ struct Mixed {
     int Vh;
     wd_precision L, H;
 
-    wd_status update(float alpha, WdVec p, WdVec q, WdVec xs, WdVec rs) const
-    {
-        double2 *part = (double2 *)ctx->red_partial;
-        if (L == WD_PREC_F32)
-            k_mx_update<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(alpha, sp_f32(p, Vh), sp_f32(q, Vh),
-                                                                          sp_f32(xs, Vh), sp_f32(rs, Vh), Vh, part);
-        else
-            k_mx_update<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(alpha, sp_f16(p, Vh), sp_f16(q, Vh),
-                                                                          sp_f32(xs, Vh), sp_f32(rs, Vh), Vh, part);
-        WD_LAUNCHED(ctx);
-        return wd_red_finish(ctx, 0);
-    }
     wd_status xpay(WdVec rs, float beta, WdVec p) const
     {
         if (L == WD_PREC_F32) k_mx_xpay<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(rs, Vh), beta, sp_f32(p, Vh), Vh);
@@ -205,13 +187,12 @@ struct Mixed {
         WD_LAUNCHED(ctx);
         return WD_OK;
     }
-    wd_status norm2(WdVec t) const
+    wd_status xpay_dev(WdVec rs, const WdMxDev *d, WdVec p) const
     {
-        double2 *part = (double2 *)ctx->red_partial;
-        if (L == WD_PREC_F32) k_mx_norm2<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(t, Vh), Vh, part);
-        else k_mx_norm2<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f16(t, Vh), Vh, part);
+        if (L == WD_PREC_F32) k_mx_xpay_dev<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(rs, Vh), d, sp_f32(p, Vh), Vh);
+        else k_mx_xpay_dev<<<site_grid(Vh), WD_RED_THREADS, 0, ctx->stream>>>(sp_f32(rs, Vh), d, sp_f16(p, Vh), Vh);
         WD_LAUNCHED(ctx);
-        return wd_red_finish(ctx, 0);
+        return WD_OK;
     }
     wd_status from_h(WdVec h, WdVec rs, WdVec p) const
     {
@@ -263,6 +244,28 @@ struct Mixed {
 };
 
 inline WdVec par_half(WdVec v, int par, int Vh) { return wd_offset(v, (int64_t)par * 12 * Vh, (int64_t)par * Vh); }
+
+// out (odd) = D_oe in (or D_oe^dag), a no-op while *stop != 0
+wd_status hop_oe_gated(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, int dag, const int *stop)
+{
+    if (in.prec == WD_PREC_F32) return wd_hop_f32(ctx, lat, in, out, nullptr, 1, dag, 1.0, 0.0, stop);
+    return wd_hop_f16(ctx, lat, in, out, nullptr, 1, dag, 1.0, 0.0, stop);
+}
+
+// a block from the context's work-buffer cache, returned on scope exit
+struct DevBlock {
+    wd_context *ctx = nullptr;
+    void *p = nullptr;
+    ~DevBlock()
+    {
+        if (p) wd_dev_free(ctx, p);
+    }
+    wd_status alloc(wd_context *c, size_t bytes)
+    {
+        ctx = c;
+        return wd_dev_alloc(c, &p, bytes);
+    }
+};
 
 }  // namespace
 
@@ -373,43 +376,68 @@ wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const dou
     double true_res = std::sqrt(ss) / norm_b;
     double ratio = ss > 0 ? std::sqrt(rr / ss) : 1.0;
     double target = prm->tol * norm_b * ratio * 0.5;
-    double rr_max = rr;
     int iters = 0;
     bool converged = true_res <= prm->tol;
+
+    // The iterations run on device scalars (WdMxDev): alpha and beta are
+    // formed by the reducing hops' last blocks, and the last block of each
+    // |r_s|^2 reduction decides whether a reliable update is due.  The host
+    // queues the number of iterations the previous residual-reduction cycle
+    // took, then reads the scalars once: iterations queued past the one that
+    // asked for an update are no-ops.
+    DevBlock dev_blk, part_blk;
+    if ((st = dev_blk.alloc(ctx, sizeof(WdMxDev))) != WD_OK) return st;
+    if ((st = part_blk.alloc(ctx, sizeof(double) * ((size_t)Vh / 64 + 2))) != WD_OK) return st;
+    WdMxDev *dev = (WdMxDev *)dev_blk.p;
+    double *partial = (double *)part_blk.p;
+    WdMxDev *sc = (WdMxDev *)ctx->state_host;
+    *sc = WdMxDev{};
+    sc->rr = sc->rr_max = rr;
+    sc->target2 = target * target;
+    sc->delta2 = delta * delta;
+    WD_CUDA(ctx, cudaMemcpyAsync(dev, sc, sizeof(WdMxDev), cudaMemcpyHostToDevice, ctx->stream));
+    int cycle = 4, since = 0;
     while (!converged && iters < prm->max_iter) {
-        if ((st = wd_apply_Mhat_v(ctx, lat, p.v, t.v, tmp_ol.v, m, 0)) != WD_OK) return st;
-        if ((st = wd_apply_Mhat_v(ctx, lat, t.v, q.v, tmp_ol.v, m, 1)) != WD_OK) return st;
-        if ((st = mx.norm2(t.v)) != WD_OK) return st;
-        if ((st = wd_red_fetch(ctx, 1, red)) != WD_OK) return st;
-        const double alpha = rr / red[0].x;
-        if ((st = mx.update((float)alpha, p.v, q.v, xs.v, rs.v)) != WD_OK) return st;
-        if ((st = wd_red_fetch(ctx, 1, red)) != WD_OK) return st;
-        double rr_new = red[0].x;
-        ++iters;
-        if (!std::isfinite(rr_new) || !std::isfinite(alpha)) {
+        const int k = std::min(std::max(1, cycle - since), prm->max_iter - iters);
+        for (int i = 0; i < k; ++i) {
+            // t = Mhat p with |t|^2 -> alpha; q = Mhat^dag t applied as the update; p = r_s + beta p
+            if ((st = hop_oe_gated(ctx, lat, p.v, tmp_ol.v, 0, &dev->stop)) != WD_OK) return st;
+            if ((st = wd_hop_lp_norm(ctx, lat, tmp_ol.v, t.v, p.v, m, dev, partial)) != WD_OK) return st;
+            if ((st = hop_oe_gated(ctx, lat, t.v, tmp_ol.v, 1, &dev->stop)) != WD_OK) return st;
+            if ((st = wd_hop_lp_update(ctx, lat, tmp_ol.v, t.v, p.v, rs.v, xs.v, m, dev, partial)) != WD_OK)
+                return st;
+            if ((st = mx.xpay_dev(rs.v, dev, p.v)) != WD_OK) return st;
+        }
+        WD_CUDA(ctx, cudaMemcpyAsync(sc, dev, sizeof(WdMxDev), cudaMemcpyDeviceToHost, ctx->stream));
+        WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        since += sc->iters - iters;
+        iters = sc->iters;
+        if (sc->stop == 2) {
             stats->iterations = iters;
             return wd_fail(ctx, WD_ERR_NAN, "mixed CG residual is not finite");
         }
-        if (rr_new < delta * delta * rr_max || std::sqrt(rr_new) <= target) {
-            const double rr_old = rr;
-            if ((st = reliable(false)) != WD_OK) return st;
-            stats->reliable_updates++;
-            true_res = std::sqrt(ss) / norm_b;
-            if (true_res <= prm->tol) {
-                converged = true;
-                break;
-            }
-            if (std::sqrt(rr_new) <= target) {
-                ratio = ss > 0 ? std::sqrt(rr / ss) : ratio;
-                target = std::fmin(target * 0.5, prm->tol * norm_b * ratio * 0.5);
-            }
-            rr_new = rr;  // continue from the recomputed residual
-            rr_max = rr;
-            rr = rr_old;
+        if (sc->stop != 1) continue;
+        // reliable update after this iteration
+        const double rr_old = sc->rr, rr_new = sc->rr_new;
+        if ((st = reliable(false)) != WD_OK) return st;
+        stats->reliable_updates++;
+        true_res = std::sqrt(ss) / norm_b;
+        if (true_res <= prm->tol) {
+            converged = true;
+            break;
         }
-        const double beta = rr_new / rr;
-        rr = rr_new;
-        if ((st = mx.xpay(rs.v, (float)beta, p.v)) != WD_OK) return st;
+        if (std::sqrt(rr_new) <= target) {
+            ratio = ss > 0 ? std::sqrt(rr / ss) : ratio;
+            target = std::fmin(target * 0.5, prm->tol * norm_b * ratio * 0.5);
+        }
+        // continue from the recomputed residual: beta = |r_s|^2 / previous |r_s|^2
+        if ((st = mx.xpay(rs.v, (float)(rr / rr_old), p.v)) != WD_OK) return st;
+        sc->rr = sc->rr_max = rr;
+        sc->target2 = target * target;
+        sc->stop = 0;
+        WD_CUDA(ctx, cudaMemcpyAsync(dev, sc, sizeof(WdMxDev), cudaMemcpyHostToDevice, ctx->stream));
+        cycle = since;
+        since = 0;
     }
     if (!converged && (st = mx.accum(xs.v, x_e)) != WD_OK) return st;
     // x_o = (b_o + D_oe x_e / 2) / a, then back to FP64

@@ -48,3 +48,23 @@ wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd
 // slot + 1, for the caller to fetch (several systems per fetch)
 wd_status wd_mx_reliable_enqueue(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
                                  const WdMxReliable &v, const WdVec *p_restart, int slot);
+
+// Device-side scalars of one mixed-precision solve.  The iteration kernels
+// read and write them, so iterations run back to back with no host wait: the
+// hop that forms t = Mhat p also reduces |t|^2 and sets alpha, the hop that
+// forms q = Mhat^dag t applies the CG update and reduces |r_s|^2, and the
+// last block of that reduction decides on the device whether a reliable
+// update is due (stop = 1) -- after which every later iteration kernel in the
+// queue returns at once until the host has run the update and cleared stop.
+struct WdMxDev {
+    double rr;        // |r_s|^2 of the current iterate
+    double rr_max;    // |r_s|^2 right after the last reliable update
+    double target2;   // an update is due once |r_s|^2 <= target2 (squared normal-residual target)
+    double delta2;    // ... or once |r_s|^2 < delta2 * rr_max
+    double tt;        // |t|^2 = |Mhat p|^2 of the running iteration
+    double rr_new;    // |r_s|^2 after the running iteration's update
+    float alpha, beta;
+    int stop;         // 0 iterate; 1 reliable update due; 2 non-finite scalar
+    int iters;        // iterations completed on the device
+    unsigned count_t, count_r;  // last-block counters of the two reductions
+};

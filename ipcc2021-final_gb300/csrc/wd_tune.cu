@@ -123,6 +123,16 @@ wd_status wd_tune_launch(wd_context *ctx, const char *kernel, int Vh, int nvaria
     return launch(best_v);  // the call's own launch, with the chosen shape
 }
 
+int wd_tune_choice(wd_context *ctx, const char *kernel, int Vh)
+{
+    Tuner &T = tuner();
+    std::lock_guard<std::mutex> lock(T.mu);
+    T.load();
+    auto it = T.best.find({ctx->device, kernel, Vh});
+    if (it != T.best.end()) return it->second;
+    return T.on() ? -1 : 0;
+}
+
 extern "C" int wd_tune_report(char *buf, int len)
 {
     Tuner &T = tuner();
