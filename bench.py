@@ -390,6 +390,7 @@ def batch_bench(wd, ctx, profile: bool = False) -> dict:
         dt, worst = solo(systems, prec, rel)
         res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt, "max_true_residual": worst}
     res["speedup_batched_vs_solo_f64"] = res["solo_f64"]["seconds"] / res["f32_inner_f64_reliable"]["seconds"]
+    res["speedup_batched_vs_solo_mixed"] = res["solo_mixed_f32"]["seconds"] / res["f32_inner_f64_reliable"]["seconds"]
     out["multi_rhs_24c48_24_sources"] = res
     for _, b, x, _ in systems:
         b.close()
@@ -404,16 +405,21 @@ def batch_bench(wd, ctx, profile: bool = False) -> dict:
         lats.append(la)
         systems.append((la, la.field(wd.gen_source(d, 300 + i)), la.field(), float(rng.uniform(0.05, 0.2))))
     res = {}
-    p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=wd.F64)
-    run(systems, p)
-    dt, stats = run(systems, p, timed=True)
-    res["batched"] = {"seconds": dt, "solves_per_s": len(systems) / dt,
-                      "iterations": [st.iterations for st in stats],
-                      "max_true_residual": max(st.true_residual for st in stats)}
-    for name, prec, rel in (("solo_mixed_f32", wd.F32, wd.F64), ("solo_f64", wd.F64, wd.F64)):
+    for name, rel in (("batched", wd.F64), ("batched_df64_reliable", wd.DF64)):
+        p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=rel)
+        run(systems, p)
+        dt, stats = run(systems, p, timed=True)
+        res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt,
+                     "iterations": [st.iterations for st in stats],
+                     "max_true_residual": max(st.true_residual for st in stats)}
+    for name, prec, rel in (("solo_mixed_f32", wd.F32, wd.F64), ("solo_mixed_f32_df64_reliable", wd.F32, wd.DF64),
+                            ("solo_f64", wd.F64, wd.F64)):
         dt, worst = solo(systems, prec, rel)
         res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt, "max_true_residual": worst}
     res["speedup_batched_vs_solo_f64"] = res["solo_f64"]["seconds"] / res["batched"]["seconds"]
+    res["speedup_batched_vs_solo_mixed"] = res["solo_mixed_f32"]["seconds"] / res["batched"]["seconds"]
+    res["speedup_batched_vs_solo_mixed_df64_reliable"] = (res["solo_mixed_f32_df64_reliable"]["seconds"]
+                                                          / res["batched_df64_reliable"]["seconds"])
     out["16_lattices_L8_to_24"] = res
     return out
 

@@ -12,13 +12,14 @@
 // delivers once and L1 serves to the rest: link traffic is divided by the
 // number of right-hand sides.
 //
-// Per-system scalars (rr, |t|^2, alpha, beta, active) live in device memory.
-// One CG iteration (4 batched hops, per-system reductions, scalar update,
-// vector updates) reads them there, so the iteration is captured once into a
-// CUDA graph and replayed; systems that converge are masked off (active = 0)
-// and their kernels return at once.  Between replays the host reads the
-// per-system residuals and runs reliable updates (double-float or FP64) for
-// the systems that need one -- the same recurrence as wd_mixed.cu.
+// Per-system scalars (rr, |t|^2, alpha, beta, active, the reliable-update
+// trigger) live in device memory.  One CG iteration (4 batched hops, two of
+// them with reducing epilogues, two per-system scalar kernels, the p update)
+// reads them there, so iterations are captured into a CUDA graph and
+// replayed; a system whose residual calls for a reliable update is masked by
+// the device at that iteration and its kernels return at once.  Between
+// replays the host reads the scalars and runs the reliable updates (double-
+// float or FP64) the device asked for -- the recurrence of wd_mixed.cu.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -37,9 +38,9 @@
 namespace {
 
 constexpr int kSites = 32;  // sites per warp (one system per warp)
-constexpr int kChunk = 8192;     // sites per reduction chunk (one block each)
+constexpr int kChunk = 8192;     // sites per xpay chunk (one block each)
 constexpr int kBatchHopVariants = 5;
-constexpr int kRelGroup = WD_RED_SLOTS / 2;  // reliable updates per host wait
+constexpr int kMaxPerGraph = 8;  // iterations queued per graph launch at most
 
 struct BGroup {
     WdGeom g;
@@ -52,16 +53,38 @@ struct BGroup {
 struct BSys {
     void *in, *out, *x;
     float *in_scale, *out_scale, *x_scale;
-    int group;
+    void *p;              // update epilogue: p (kernel storage) and its scales
+    float *p_scale;
+    float4 *rs, *xs;      // update epilogue: FP32 r_s and x_s
+    int part0, nparts;    // this system's warp partials: [part0, part0 + nparts)
 };
+
+// Per-system scalars of the batched CG, in device memory.  The iteration
+// kernels read and write them; after a graph launch the host reads the
+// whole array once.  A system whose |r_s|^2 has fallen by delta^2 since its
+// last reliable update (or reached its target) is masked (active = 0,
+// wait = 1) by the device at once; later iterations skip it until the host
+// has run its reliable update.
+struct BScal {
+    double rr, rr_max, target2, tt, rr_new;
+    float alpha, beta;
+    int active;  // 1: iterating
+    int wait;    // 1: reliable update due; 2: non-finite scalar
+    int iters;
+    int pad;
+};
+
+// epilogue of a batched hop: plain (h0, h2), |t|^2 (h1), CG update (h3)
+enum { kBEpiPlain = 0, kBEpiNorm = 1, kBEpiUpdate = 2 };
 
 struct BTable {
     const BGroup *groups;
     int ngroups;
     const BSys *sys;
-    const float *alpha;  // per system
+    const float *alpha;  // per system: the hop's output scale and x coefficient
     const float *beta;
-    const int *active;
+    BScal *sc;
+    double *partial;     // warp partials of the reducing epilogues
     int cb;
 };
 
@@ -96,26 +119,61 @@ __device__ __forceinline__ int find_group(const BGroup *groups, int ngroups, int
     return lo;
 }
 
-// out = alpha acc (+ beta x) of system sys at site s (per-system scalars)
 template <bool F16>
-__device__ __forceinline__ void batch_epilogue(const BTable &t, const BSys &S, int sys, int s, int Vh,
-                                               const float2 *acc)
+struct BSp {
+    using T = std::conditional_t<F16, SpF16, SpF32>;
+    static __device__ __forceinline__ T make(void *p, float *scale, int Vh)
+    {
+        if constexpr (F16) return SpF16{(uint4 *)p, scale, Vh};
+        else return SpF32{(float4 *)p, Vh};
+    }
+};
+
+// r = alpha acc (+ beta x) of system sys at site s, then the epilogue EPI;
+// returns the site's contribution to the reduction (0 for plain)
+template <bool F16, int EPI>
+__device__ __forceinline__ float batch_epilogue(const BTable &t, const BSys &S, int sys, int s, int Vh,
+                                                const float2 *acc)
 {
     const float al = t.alpha[sys], be = t.beta[sys];
-    float2 r12[12];
+    float2 r[12];
     if (S.x) {
         float2 xv[12];
         float bx = be;  // beta times the x site's scale
         if constexpr (F16) bx *= SpF16{(uint4 *)S.x, S.x_scale, Vh}.load_raw(s, xv);
         else SpF32{(float4 *)S.x, Vh}.load(s, xv);
 #pragma unroll
-        for (int c = 0; c < 12; ++c) r12[c] = c_axpby(al, acc[c], bx, xv[c]);
+        for (int c = 0; c < 12; ++c) r[c] = c_axpby(al, acc[c], bx, xv[c]);
     } else {
 #pragma unroll
-        for (int c = 0; c < 12; ++c) r12[c] = c_scale(acc[c], al);
+        for (int c = 0; c < 12; ++c) r[c] = c_scale(acc[c], al);
     }
-    if constexpr (F16) SpF16{(uint4 *)S.out, S.out_scale, Vh}.store(s, r12);
-    else SpF32{(float4 *)S.out, Vh}.store(s, r12);
+    float n = 0.f;
+    if constexpr (EPI != kBEpiUpdate) {
+        if constexpr (EPI == kBEpiNorm) {
+#pragma unroll
+            for (int c = 0; c < 12; ++c) n = fmaf(r[c].x, r[c].x, fmaf(r[c].y, r[c].y, n));
+        }
+        BSp<F16>::make(S.out, S.out_scale, Vh).store(s, r);
+    } else {
+        // q = r is not stored: r_s -= alpha q, x_s += alpha p
+        const float a = t.sc[sys].alpha;
+        const SpF32 rs{S.rs, Vh}, xs{S.xs, Vh};
+        float2 v[12];
+        rs.load(s, v);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) {
+            v[c] = make_float2(fmaf(-a, r[c].x, v[c].x), fmaf(-a, r[c].y, v[c].y));
+            n = fmaf(v[c].x, v[c].x, fmaf(v[c].y, v[c].y, n));
+        }
+        rs.store(s, v);
+        BSp<F16>::make(S.p, S.p_scale, Vh).load(s, r);
+        xs.load(s, v);
+#pragma unroll
+        for (int c = 0; c < 12; ++c) v[c] = make_float2(fmaf(a, r[c].x, v[c].x), fmaf(a, r[c].y, v[c].y));
+        xs.store(s, v);
+    }
+    return n;
 }
 
 // the operands of one system: its input spinor and the group's links
@@ -141,152 +199,107 @@ __device__ __forceinline__ auto batch_policy(const BTable &t, const BGroup &G, c
     }
 }
 
-// SYS systems (warps) per block sharing the block's sites; MINB blocks per SM
-// (0: no bound) bound the registers (the kernel is latency-bound: DRAM bytes per
-// system-site sit at the link-shared minimum, so occupancy sets its speed)
-template <bool DAG, bool F16, int SYS, int MINB>
+// SYS systems (warps) per block sharing the block's 32 sites; MINB blocks per
+// SM (0: no bound) bound the registers.  A warp is one system's 32
+// consecutive sites, so a reducing epilogue writes one partial per warp.
+template <bool DAG, bool F16, int SYS, int MINB, int EPI>
 __global__ void __launch_bounds__(kSites * SYS, MINB) k_batch_hop(const BTable t)
 {
     const int gi = find_group(t.groups, t.ngroups, blockIdx.x);
     const BGroup &G = t.groups[gi];
     const int r = blockIdx.y * SYS + (threadIdx.x / kSites);
-    const int s = (blockIdx.x - G.block_start) * kSites + (threadIdx.x % kSites);
-    if (r >= G.nsys || s >= G.g.Vh) return;
+    if (r >= G.nsys) return;  // whole warps
     const int sys = G.first_sys + r;
-    if (!t.active[sys]) return;
+    if (!t.sc[sys].active) return;
+    const int blk = blockIdx.x - G.block_start;
+    const int s = blk * kSites + (threadIdx.x % kSites);
     const BSys &S = t.sys[sys];
-    float2 acc[12];
-    wd_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
-    batch_epilogue<F16>(t, S, sys, s, G.g.Vh, acc);
+    float v = 0.f;
+    if (s < G.g.Vh) {
+        float2 acc[12];
+        wd_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
+        v = batch_epilogue<F16, EPI>(t, S, sys, s, G.g.Vh, acc);
+    }
+    if constexpr (EPI != kBEpiPlain) {
+        const double d = wd_warp_sum((double)v);
+        if ((threadIdx.x & 31) == 0) t.partial[S.part0 + blk] = d;
+    }
 }
 
-// ---------------------------------------------------------- batched BLAS
-// per-system vectors: p, t, q (kernel storage), r_s, x_s (FP32), all even blocks
+// per-system vectors for the xpay pass (even blocks)
 struct BVec {
-    void *p, *t, *q;
-    float *p_scale, *t_scale, *q_scale;
-    float4 *rs, *xs;
+    void *p;
+    float *p_scale;
+    float4 *rs;
     int Vh;
-    int chunk0;  // first reduction chunk of this system
+    int chunk0;  // first xpay chunk of this system
 };
 
-struct BState {
-    double *rr;      // |r_s|^2 (sloppy) per system
-    double *tt;      // |t|^2
-    float *alpha, *beta;
-    int *active;
-    double *partial; // per reduction chunk
-    int *chunk_sys;  // system of each reduction chunk
-    int nchunks;
-};
-
-__device__ __forceinline__ dfr sq_acc(dfr acc, float2 v)
-{
-    return df_madd(df_madd(acc, dfr{v.x, 0.f}, dfr{v.x, 0.f}), dfr{v.y, 0.f}, dfr{v.y, 0.f});
-}
-
-// one block per chunk of kChunk... sites of one system
+// p = r_s + beta p for the iterating systems
 template <bool F16>
-__global__ void __launch_bounds__(WD_RED_THREADS) k_batch_norm_t(const BVec *v, BState st)
+__global__ void __launch_bounds__(WD_RED_THREADS) k_batch_xpay(const BVec *v, const int *chunk_sys, const BScal *sc)
 {
     const int c = blockIdx.x;
-    const int sys = st.chunk_sys[c];
-    dfr acc{0.f, 0.f};
-    if (st.active[sys]) {
-        const BVec &B = v[sys];
-        const int s0 = (c - B.chunk0) * kChunk;
-        const int s1 = min(s0 + kChunk, B.Vh);
-        for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            float2 tv[12];
-            if constexpr (F16) SpF16{(uint4 *)B.t, B.t_scale, B.Vh}.load(s, tv);
-            else SpF32{(float4 *)B.t, B.Vh}.load(s, tv);
-#pragma unroll
-            for (int k = 0; k < 12; ++k) acc = sq_acc(acc, tv[k]);
-        }
-    }
-    double2 *part = reinterpret_cast<double2 *>(st.partial);
-    wd_block_partial(df_value(acc), 0.0, part);
-}
-
-// x_s += alpha p; r_s -= alpha q; chunk partial of |r_s|^2
-template <bool F16>
-__global__ void __launch_bounds__(WD_RED_THREADS) k_batch_update(const BVec *v, BState st)
-{
-    const int c = blockIdx.x;
-    const int sys = st.chunk_sys[c];
-    dfr acc{0.f, 0.f};
-    if (st.active[sys]) {
-        const BVec &B = v[sys];
-        const float a = st.alpha[sys];
-        const int s0 = (c - B.chunk0) * kChunk;
-        const int s1 = min(s0 + kChunk, B.Vh);
-        for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-            float2 pv[12], qv[12], xv[12], rv[12];
-            if constexpr (F16) {
-                SpF16{(uint4 *)B.p, B.p_scale, B.Vh}.load(s, pv);
-                SpF16{(uint4 *)B.q, B.q_scale, B.Vh}.load(s, qv);
-            } else {
-                SpF32{(float4 *)B.p, B.Vh}.load(s, pv);
-                SpF32{(float4 *)B.q, B.Vh}.load(s, qv);
-            }
-            const SpF32 xs{B.xs, B.Vh}, rs{B.rs, B.Vh};
-            xs.load(s, xv);
-            rs.load(s, rv);
-#pragma unroll
-            for (int k = 0; k < 12; ++k) {
-                xv[k] = make_float2(fmaf(a, pv[k].x, xv[k].x), fmaf(a, pv[k].y, xv[k].y));
-                rv[k] = make_float2(fmaf(-a, qv[k].x, rv[k].x), fmaf(-a, qv[k].y, rv[k].y));
-                acc = sq_acc(acc, rv[k]);
-            }
-            xs.store(s, xv);
-            rs.store(s, rv);
-        }
-    }
-    double2 *part = reinterpret_cast<double2 *>(st.partial);
-    wd_block_partial(df_value(acc), 0.0, part);
-}
-
-// p = r_s + beta p
-template <bool F16>
-__global__ void __launch_bounds__(WD_RED_THREADS) k_batch_xpay(const BVec *v, BState st)
-{
-    const int c = blockIdx.x;
-    const int sys = st.chunk_sys[c];
-    if (!st.active[sys]) return;
+    const int sys = chunk_sys[c];
+    if (!sc[sys].active) return;
     const BVec &B = v[sys];
-    const float be = st.beta[sys];
+    const float be = sc[sys].beta;
     const int s0 = (c - B.chunk0) * kChunk;
     const int s1 = min(s0 + kChunk, B.Vh);
     for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
         float2 pv[12], rv[12];
         SpF32{B.rs, B.Vh}.load(s, rv);
-        if constexpr (F16) SpF16{(uint4 *)B.p, B.p_scale, B.Vh}.load(s, pv);
-        else SpF32{(float4 *)B.p, B.Vh}.load(s, pv);
+        BSp<F16>::make(B.p, B.p_scale, B.Vh).load(s, pv);
 #pragma unroll
         for (int k = 0; k < 12; ++k) pv[k] = make_float2(fmaf(be, pv[k].x, rv[k].x), fmaf(be, pv[k].y, rv[k].y));
-        if constexpr (F16) SpF16{(uint4 *)B.p, B.p_scale, B.Vh}.store(s, pv);
-        else SpF32{(float4 *)B.p, B.Vh}.store(s, pv);
+        BSp<F16>::make(B.p, B.p_scale, B.Vh).store(s, pv);
     }
 }
 
-// per-system sums of chunk partials (fixed order) -> out[sys]; then scalars
-// mode 0: tt = sum; alpha = rr / tt
-// mode 1: rr_new = sum; beta = rr_new / rr; rr = rr_new
-__global__ void k_batch_scalars(const BVec *v, BState st, int nsys, int mode)
+// One block per system folds its warp partials in a fixed order.
+// mode 0 (|t|^2): alpha = rr / tt.
+// mode 1 (|r_s|^2 after the update): the reliable-update rule -- mask the
+// system and flag it when |r_s|^2 < delta2 rr_max or <= target2, else
+// beta = rr_new / rr, rr = rr_new.
+constexpr int kScalThreads = 128;
+__global__ void __launch_bounds__(kScalThreads) k_batch_scalars(const BSys *sys_tab, BScal *sc, const double *partial,
+                                                                int mode, double delta2)
 {
-    const int sys = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sys >= nsys || !st.active[sys]) return;
-    const BVec &B = v[sys];
-    const int nch = (B.Vh + kChunk - 1) / kChunk;
-    const double2 *part = reinterpret_cast<const double2 *>(st.partial);
-    double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += part[B.chunk0 + c].x;
+    const int sys = blockIdx.x;
+    if (!sc[sys].active) return;  // the whole block
+    const BSys &S = sys_tab[sys];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < S.nparts; i += kScalThreads) v += partial[S.part0 + i];
+    v = wd_warp_sum(v);
+    __shared__ double sw[kScalThreads / 32];
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kScalThreads / 32; ++w) v += sw[w];
+    BScal &c = sc[sys];
     if (mode == 0) {
-        st.tt[sys] = s;
-        st.alpha[sys] = s > 0 ? (float)(st.rr[sys] / s) : 0.f;
+        c.tt = v;
+        if (!(v > 0.0) || !isfinite(v)) {
+            c.wait = 2;
+            c.active = 0;
+            return;
+        }
+        c.alpha = (float)(c.rr / v);
+        return;
+    }
+    c.rr_new = v;
+    c.iters += 1;
+    if (!isfinite(v)) {
+        c.wait = 2;
+        c.active = 0;
+    } else if (v < delta2 * c.rr_max || v <= c.target2) {
+        c.wait = 1;
+        c.active = 0;
     } else {
-        st.beta[sys] = st.rr[sys] > 0 ? (float)(s / st.rr[sys]) : 0.f;
-        st.rr[sys] = s;
+        c.beta = (float)(v / c.rr);
+        c.rr = v;
     }
 }
 
@@ -296,21 +309,30 @@ __global__ void k_batch_scalars(const BVec *v, BState st, int nsys, int mode)
 //
 // BatchEngine keeps a changing set of systems iterating together.  Systems
 // are added with add() (set-up and the first reliable update run at once)
-// and step() advances every active system by one captured graph of
-// per_graph iterations, then reads the per-system residuals, runs reliable
-// updates where due and retires converged systems (writes the FP64 solution
-// and frees their buffers).  A retired system is first masked in the device
-// tables; the tables and the graph are rebuilt (compacted) when systems join
-// or when masked systems make up half of the tables.
+// and step() advances every active system by one captured graph of K
+// iterations.  The iterations run entirely on per-system device scalars
+// (BScal): the hop forming t = Mhat p reduces |t|^2, the hop forming
+// q = Mhat^dag t applies the CG update in place of storing q, and the
+// scalar kernels set alpha and beta and mask a system the moment its
+// residual calls for a reliable update, so K need not match any system's
+// cycle.  After the graph the host reads the scalars once, runs the due
+// reliable updates (their results land in a device array read with one more
+// wait), retires converged systems (writes the FP64 solution and frees their
+// buffers) and re-arms the rest.  K is the shortest expected remaining cycle
+// (the previous cycle's length) of the iterating systems, at most
+// kMaxPerGraph.  Retired systems are masked; the tables and graphs are
+// rebuilt (compacted) when systems join or when masked systems make up half
+// of the tables.
 
 namespace {
 
 struct SysBufs {
-    WdVecBuf p, t, q, tmp_o, rs, xs;               // kernel storage / FP32
-    WdVecBuf hs, hx, bhat, s_e, r_h, t_h, tmp_oh;  // high precision
+    WdVecBuf p, t, tmp_o, rs, xs;       // kernel storage / FP32
+    WdVecBuf hs, hx, bhat, r_h, tmp_oh;  // high precision
+    WdVecBuf rel;                        // reliable-update reduction scratch (doubles)
     void release()
     {
-        for (WdVecBuf *b : {&p, &t, &q, &tmp_o, &rs, &xs, &hs, &hx, &bhat, &s_e, &r_h, &t_h, &tmp_oh}) b->release();
+        for (WdVecBuf *b : {&p, &t, &tmp_o, &rs, &xs, &hs, &hx, &bhat, &r_h, &tmp_oh, &rel}) b->release();
     }
 };
 
@@ -330,15 +352,20 @@ struct DevArray {
         n = 0;
         ctx = nullptr;
     }
-    wd_status put(wd_context *c, const std::vector<T> &h)
+    wd_status reserve(wd_context *c, size_t count)
     {
-        if (h.size() > n) {
+        if (count > n) {
             release();
             ctx = c;
-            n = h.size();
-            wd_status st = wd_dev_alloc(c, (void **)&p, n * sizeof(T));
-            if (st != WD_OK) return st;
+            n = count;
+            return wd_dev_alloc(c, (void **)&p, n * sizeof(T));
         }
+        return WD_OK;
+    }
+    wd_status put(wd_context *c, const std::vector<T> &h)
+    {
+        wd_status st = reserve(c, h.size());
+        if (st != WD_OK) return st;
         if (!h.empty())
             WD_CUDA(c, cudaMemcpyAsync(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, c->stream));
         return WD_OK;
@@ -354,6 +381,7 @@ struct EngineSys {
     SysBufs B;
     double norm_b = 1, rr = 0, rr_max = 0, target = 0, ratio = 1, true_res = 1;
     int updates = 0, iters = 0;
+    int since = 0, cycle = 4;  // iterations since the last reliable update; length of the previous cycle
     bool active = true;
 };
 
@@ -362,16 +390,23 @@ size_t system_bytes(const wd_lattice *lat, wd_precision L, wd_precision H)
 {
     const size_t nh = (size_t)12 * lat->g.Vh;
     size_t lbytes = nh * wd_entry_bytes(L) + (L == WD_PREC_F16 ? (size_t)lat->g.Vh * 4 : 0);
-    return 4 * lbytes + 2 * nh * 8 + 5 * nh * wd_entry_bytes(H) + 2 * 2 * nh * wd_entry_bytes(H);
+    return 3 * lbytes + 2 * nh * 8 + 3 * nh * wd_entry_bytes(H) + 2 * 2 * nh * wd_entry_bytes(H);
 }
 
 class BatchEngine {
   public:
-    BatchEngine(wd_context *ctx, wd_precision L, wd_precision H, double delta, int per_graph, int max_iter)
-        : ctx_(ctx), L_(L), H_(H), delta_(delta), per_graph_(per_graph), max_iter_(max_iter)
+    BatchEngine(wd_context *ctx, wd_precision L, wd_precision H, double delta, int max_iter)
+        : ctx_(ctx), L_(L), H_(H), delta_(delta), max_iter_(max_iter)
     {
     }
-    ~BatchEngine() { drop_graph(); }
+    ~BatchEngine()
+    {
+        drop_graphs();
+        for (auto &e : rel_ev_)
+            if (e) cudaEventDestroy(e);
+        for (auto &q : rel_stream_)
+            if (q) cudaStreamDestroy(q);
+    }
 
     size_t active() const
     {
@@ -396,7 +431,7 @@ class BatchEngine {
     wd_context *ctx_;
     wd_precision L_, H_;
     double delta_;
-    int per_graph_, max_iter_;
+    int max_iter_;
     std::vector<std::unique_ptr<EngineSys>> sys_;
     std::vector<int> retired_;
     bool rebuild_ = true, scalars_dirty_ = false;
@@ -405,25 +440,34 @@ class BatchEngine {
     DevArray<BSys> d_sys_[4];
     DevArray<float> d_alpha_[4], d_beta_[4];
     DevArray<BVec> d_vec_;
-    DevArray<double> d_rr_, d_tt_, d_partial_;
-    DevArray<float> d_a_, d_b_;
-    DevArray<int> d_active_, d_chunk_sys_;
+    DevArray<BScal> d_sc_;
+    DevArray<double> d_partial_, d_rel_;
+    DevArray<int> d_chunk_sys_;
+    std::vector<BScal> h_sc_;
     int grid_x_ = 0, nchunks_ = 0, ngroups_ = 0, max_group_sys_ = 1;
     int hop_variant_ = 0;  // launch shape of the batched hop (tuned in rebuild)
-    cudaGraphExec_t exec_ = nullptr;
-    uint64_t kernels_per_graph_ = 0;
+    std::map<int, cudaGraphExec_t> graphs_;  // K -> K captured iterations
+    uint64_t kernels_per_iter_ = 0;
+    // reliable updates due at the same step run on up to kRelStreams streams
+    // at once (small lattices alone cannot fill the GPU)
+    static constexpr int kRelStreams = 8;
+    cudaStream_t rel_stream_[kRelStreams] = {};
+    cudaEvent_t rel_ev_[kRelStreams + 1] = {};
+    wd_status rel_streams();
+    wd_status reliable_round(const std::vector<int> &upd);
 
-    void drop_graph()
+    void drop_graphs()
     {
-        if (exec_) cudaGraphExecDestroy(exec_);
-        exec_ = nullptr;
+        for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
+        graphs_.clear();
     }
     wd_status reliable(EngineSys &s, bool reset_p, double *rr, double *ss);
-    wd_status reliable_enqueue(EngineSys &s, bool reset_p, int slot);
+    wd_status reliable_enqueue(EngineSys &s, bool reset_p, double *rr_dev, double *ss_dev);
     wd_status finish(EngineSys &s);
     wd_status rebuild();
-    wd_status iteration(const BState &bst);
-    wd_status hop(int h, int cb, int dag, int variant);
+    wd_status graph(int k, cudaGraphExec_t *exec);
+    wd_status iteration();
+    wd_status hop(int h, int cb, int dag, int variant, int epi);
     wd_status upload_scalars();
 };
 
@@ -439,7 +483,8 @@ static inline void slices(EngineSys &s, WdVec &b_e, WdVec &b_o, WdVec &x_e, WdVe
 // reliable update: x_e += x_s; s = bhat - Mhat x_e; r_s = Mhat^dag s (FP32); p <- r_s on a restart
 wd_status BatchEngine::reliable(EngineSys &s, bool reset_p, double *rr, double *ss)
 {
-    wd_status e = reliable_enqueue(s, reset_p, 0);
+    double2 *res = (double2 *)ctx_->red_partial + WD_RED_BLOCKS;
+    wd_status e = reliable_enqueue(s, reset_p, &res[0].x, &res[1].x);
     if (e != WD_OK) return e;
     double2 red[2];
     if ((e = wd_red_fetch(ctx_, 2, red)) != WD_OK) return e;
@@ -448,13 +493,14 @@ wd_status BatchEngine::reliable(EngineSys &s, bool reset_p, double *rr, double *
     return WD_OK;
 }
 
-wd_status BatchEngine::reliable_enqueue(EngineSys &s, bool reset_p, int slot)
+wd_status BatchEngine::reliable_enqueue(EngineSys &s, bool reset_p, double *rr_dev, double *ss_dev)
 {
     SysBufs &B = s.B;
     WdVec b_e, b_o, x_e, x_o;
     slices(s, b_e, b_o, x_e, x_o);
-    const WdMxReliable rv{B.xs.v, x_e, B.bhat.v, B.t_h.v, B.s_e.v, B.tmp_oh.v, B.r_h.v, B.rs.v};
-    return wd_mx_reliable_enqueue(ctx_, s.lat, s.mass, L_, H_, rv, reset_p ? &B.p.v : nullptr, slot);
+    const WdMxReliable rv{B.xs.v, x_e, B.bhat.v, B.tmp_oh.v, B.r_h.v, B.rs.v};
+    return wd_mx_reliable_enqueue(ctx_, s.lat, s.mass, L_, H_, rv, reset_p ? &B.p.v : nullptr, rr_dev, ss_dev,
+                                  (double *)B.rel.v.p);
 }
 
 wd_status BatchEngine::add(int tag, const wd_lattice *lat, const double2 *src, double2 *dest, double mass,
@@ -469,14 +515,16 @@ wd_status BatchEngine::add(int tag, const wd_lattice *lat, const double2 *src, d
     const double a = 4.0 + mass;
     SysBufs &B = s.B;
     wd_status st;
-    for (WdVecBuf *b : {&B.p, &B.t, &B.q, &B.tmp_o})
+    for (WdVecBuf *b : {&B.p, &B.t, &B.tmp_o})
         if ((st = wd_vec_alloc(ctx_, *b, L_, nh)) != WD_OK) return st;
     for (WdVecBuf *b : {&B.rs, &B.xs})
         if ((st = wd_vec_alloc(ctx_, *b, WD_PREC_F32, nh)) != WD_OK) return st;
-    for (WdVecBuf *b : {&B.bhat, &B.s_e, &B.r_h, &B.t_h, &B.tmp_oh})
+    for (WdVecBuf *b : {&B.bhat, &B.r_h, &B.tmp_oh})
         if ((st = wd_vec_alloc(ctx_, *b, H_, nh)) != WD_OK) return st;
     for (WdVecBuf *b : {&B.hs, &B.hx})
         if ((st = wd_vec_alloc(ctx_, *b, H_, 2 * nh)) != WD_OK) return st;
+    if ((st = wd_vec_alloc(ctx_, B.rel, WD_PREC_F64, (int64_t)(wd_mx_reliable_scratch_doubles(Vh) + 1) / 2)) != WD_OK)
+        return st;
     if ((st = wd_lattice_gauge_lp(ctx_, lat, L_)) != WD_OK) return st;
     if (H_ == WD_PREC_DF64) {
         if ((st = wd_convert_f64_to_df(ctx_, src, (float4 *)B.hs.v.p, 2 * nh)) != WD_OK) return st;
@@ -538,7 +586,7 @@ wd_status BatchEngine::finish(EngineSys &s)
 
 wd_status BatchEngine::rebuild()
 {
-    drop_graph();
+    drop_graphs();
     // drop retired systems, group by lattice (stable)
     std::vector<std::unique_ptr<EngineSys>> keep;
     for (auto &s : sys_)
@@ -554,6 +602,7 @@ wd_status BatchEngine::rebuild()
     if (nsys == 0) return WD_OK;
     const bool f16 = L_ == WD_PREC_F16;
     std::vector<BGroup> groups;
+    std::vector<int> sys_group(nsys);
     int blocks = 0;
     for (int k = 0; k < nsys; ++k) {
         if (k == 0 || sys_[k]->lat != sys_[k - 1]->lat) {
@@ -567,6 +616,7 @@ wd_status BatchEngine::rebuild()
             groups.push_back(G);
         }
         groups.back().nsys++;
+        sys_group[k] = (int)groups.size() - 1;
     }
     grid_x_ = blocks;
     max_group_sys_ = 1;
@@ -574,18 +624,19 @@ wd_status BatchEngine::rebuild()
     ngroups_ = (int)groups.size();
     std::vector<BVec> bvec(nsys);
     std::vector<int> chunk_sys;
-    std::vector<double> rr(nsys);
-    std::vector<int> act(nsys, 1);
+    std::vector<int> part0(nsys), nparts(nsys);
+    int parts = 0;
     for (int k = 0; k < nsys; ++k) {
         SysBufs &B = sys_[k]->B;
         BVec &v = bvec[k];
-        v.p = B.p.v.p, v.t = B.t.v.p, v.q = B.q.v.p;
-        v.p_scale = B.p.v.scale, v.t_scale = B.t.v.scale, v.q_scale = B.q.v.scale;
-        v.rs = (float4 *)B.rs.v.p, v.xs = (float4 *)B.xs.v.p;
+        v.p = B.p.v.p, v.p_scale = B.p.v.scale;
+        v.rs = (float4 *)B.rs.v.p;
         v.Vh = sys_[k]->lat->g.Vh;
         v.chunk0 = (int)chunk_sys.size();
         for (int c = 0; c < (v.Vh + kChunk - 1) / kChunk; ++c) chunk_sys.push_back(k);
-        rr[k] = sys_[k]->rr;
+        part0[k] = parts;
+        nparts[k] = (v.Vh + kSites - 1) / kSites;
+        parts += nparts[k];
     }
     nchunks_ = (int)chunk_sys.size();
     wd_status st;
@@ -596,12 +647,14 @@ wd_status BatchEngine::rebuild()
         for (int k = 0; k < nsys; ++k) {
             const double a = 4.0 + sys_[k]->mass;
             const SysBufs &B = sys_[k]->B;
-            // h = 0: p -> tmp_o (cb 1); 1: tmp_o -> t with x = p (cb 0); 2: t -> tmp_o; 3: tmp_o -> q with x = t
+            // h = 0: p -> tmp_o (cb 1); 1: tmp_o -> t with x = p (cb 0); 2: t -> tmp_o; 3: tmp_o -> (update) with x = t
             const WdVec *vin[4] = {&B.p.v, &B.tmp_o.v, &B.t.v, &B.tmp_o.v};
-            const WdVec *vout[4] = {&B.tmp_o.v, &B.t.v, &B.tmp_o.v, &B.q.v};
+            const WdVec *vout[4] = {&B.tmp_o.v, &B.t.v, &B.tmp_o.v, &B.t.v};
             const WdVec *vx[4] = {nullptr, &B.p.v, nullptr, &B.t.v};
-            tab[k] = BSys{vin[h]->p, vout[h]->p, vx[h] ? vx[h]->p : nullptr, vin[h]->scale, vout[h]->scale,
-                          vx[h] ? vx[h]->scale : nullptr, 0};
+            BSys &S = tab[k];
+            S = BSys{vin[h]->p, vout[h]->p, vx[h] ? vx[h]->p : nullptr, vin[h]->scale, vout[h]->scale,
+                     vx[h] ? vx[h]->scale : nullptr, B.p.v.p, B.p.v.scale, (float4 *)B.rs.v.p, (float4 *)B.xs.v.p,
+                     part0[k], nparts[k]};
             al[k] = (h % 2 == 0) ? 1.0f : (float)(-0.25 / a);
             be[k] = (h % 2 == 0) ? 0.0f : (float)a;
         }
@@ -609,16 +662,11 @@ wd_status BatchEngine::rebuild()
         if ((st = d_alpha_[h].put(ctx_, al)) != WD_OK) return st;
         if ((st = d_beta_[h].put(ctx_, be)) != WD_OK) return st;
     }
-    std::vector<double> zeros_d(nsys, 0.0), zeros_p(2 * (size_t)nchunks_, 0.0);
-    std::vector<float> zeros_f(nsys, 0.f);
     if ((st = d_vec_.put(ctx_, bvec)) != WD_OK) return st;
-    if ((st = d_rr_.put(ctx_, rr)) != WD_OK) return st;
-    if ((st = d_tt_.put(ctx_, zeros_d)) != WD_OK) return st;
-    if ((st = d_a_.put(ctx_, zeros_f)) != WD_OK) return st;
-    if ((st = d_b_.put(ctx_, zeros_f)) != WD_OK) return st;
-    if ((st = d_active_.put(ctx_, act)) != WD_OK) return st;
-    if ((st = d_partial_.put(ctx_, zeros_p)) != WD_OK) return st;
     if ((st = d_chunk_sys_.put(ctx_, chunk_sys)) != WD_OK) return st;
+    if ((st = d_partial_.reserve(ctx_, parts)) != WD_OK) return st;
+    if ((st = d_rel_.reserve(ctx_, 2 * (size_t)nsys)) != WD_OK) return st;
+    if ((st = upload_scalars()) != WD_OK) return st;
 
     // launch shape of the batched hop, timed on its first operator (p -> the
     // odd scratch, which every iteration rewrites before reading) outside the
@@ -627,57 +675,75 @@ wd_status BatchEngine::rebuild()
     for (const BGroup &G : groups) sites += (int64_t)G.g.Vh * G.nsys;
     int bucket = 1;
     while ((int64_t)bucket < sites && bucket < (1 << 30)) bucket <<= 1;
-    if ((st = wd_tune_launch(ctx_, f16 ? "batch_hop_f16" : "batch_hop_f32", bucket, kBatchHopVariants,
-                             [&](int v) -> wd_status {
-                                 hop_variant_ = v;
-                                 return hop(0, 1, 0, v);
-                             })) != WD_OK)
-        return st;
+    return wd_tune_launch(ctx_, f16 ? "batch_hop_f16" : "batch_hop_f32", bucket, kBatchHopVariants,
+                          [&](int v) -> wd_status {
+                              hop_variant_ = v;
+                              return hop(0, 1, 0, v, kBEpiPlain);
+                          });
+}
 
-    // capture per_graph iterations
-    const BState bst{d_rr_.p, d_tt_.p, d_a_.p, d_b_.p, d_active_.p, d_partial_.p, d_chunk_sys_.p, nchunks_};
+// k captured iterations (built on first use after each rebuild)
+wd_status BatchEngine::graph(int k, cudaGraphExec_t *exec)
+{
+    auto it = graphs_.find(k);
+    if (it != graphs_.end()) {
+        *exec = it->second;
+        return WD_OK;
+    }
     const uint64_t before = ctx_->launches;
-    cudaGraph_t graph = nullptr;
+    cudaGraph_t g = nullptr;
     WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
     WD_CUDA(ctx_, cudaStreamBeginCapture(ctx_->stream, cudaStreamCaptureModeThreadLocal));
     wd_status cap = WD_OK;
-    for (int k = 0; k < per_graph_ && cap == WD_OK; ++k) cap = iteration(bst);
-    const cudaError_t ce = cudaStreamEndCapture(ctx_->stream, &graph);
-    kernels_per_graph_ = ctx_->launches - before;
+    for (int i = 0; i < k && cap == WD_OK; ++i) cap = iteration();
+    const cudaError_t ce = cudaStreamEndCapture(ctx_->stream, &g);
+    kernels_per_iter_ = (ctx_->launches - before) / (uint64_t)k;
     ctx_->launches = before;  // counted per replay
     if (cap != WD_OK) {
-        if (graph) cudaGraphDestroy(graph);
+        if (g) cudaGraphDestroy(g);
         return cap;
     }
     if (ce != cudaSuccess) return wd_cuda_check(ctx_, ce, "cudaStreamEndCapture");
-    const cudaError_t ie = cudaGraphInstantiate(&exec_, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess) {
-        exec_ = nullptr;
-        return wd_cuda_check(ctx_, ie, "cudaGraphInstantiate");
-    }
+    cudaGraphExec_t e = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&e, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return wd_cuda_check(ctx_, ie, "cudaGraphInstantiate");
+    graphs_[k] = e;
+    *exec = e;
     return WD_OK;
 }
 
-// batched hop h (operand table h) with launch variant v: (systems per block,
-// min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12), (4, none).  A whole
-// 24-source solve at 24^3x48 (GB300, seconds): FP32 inner 0.298 / 0.270 /
-// 0.265 / 0.268 / 0.274, FP16 inner 0.263 / 0.247 / 0.244 / 0.245 / 0.256.
-// Dropped: the hop with each thread's operands staged in shared memory by
-// cp.async, with 4 or 2 systems per block (FP32 0.276 / 0.279, FP16 0.243 /
-// 0.243: no gain; the block's systems already share links through L1).
-wd_status BatchEngine::hop(int h, int cb, int dag, int v)
+// batched hop h (operand table h) with launch variant v and epilogue epi:
+// (systems per block, min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12), (4, none).
+// A whole 24-source solve at 24^3x48 before the epilogue fusion (GB300,
+// seconds): FP32 inner 0.298 / 0.270 / 0.265 / 0.268 / 0.274, FP16 inner
+// 0.263 / 0.247 / 0.244 / 0.245 / 0.256.  Dropped: the hop with each thread's
+// operands staged in shared memory by cp.async, with 4 or 2 systems per block
+// (FP32 0.276 / 0.279, FP16 0.243 / 0.243: no gain; the block's systems
+// already share links through L1).
+wd_status BatchEngine::hop(int h, int cb, int dag, int v, int epi)
 {
-    const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_active_.p, cb};
+    const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_sc_.p, d_partial_.p, cb};
     auto run = [&](auto sys, auto minb) -> wd_status {
         constexpr int S = decltype(sys)::value, M = decltype(minb)::value;
         const dim3 grid(grid_x_, (max_group_sys_ + S - 1) / S);
+        auto go = [&](auto f16, auto e) {
+            constexpr bool F = decltype(f16)::value;
+            constexpr int E = decltype(e)::value;
+            if (dag) k_batch_hop<true, F, S, M, E><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+            else k_batch_hop<false, F, S, M, E><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+        };
+        using E0 = std::integral_constant<int, kBEpiPlain>;
+        using E1 = std::integral_constant<int, kBEpiNorm>;
+        using E2 = std::integral_constant<int, kBEpiUpdate>;
         if (L_ == WD_PREC_F16) {
-            if (dag) k_batch_hop<true, true, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
-            else k_batch_hop<false, true, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+            if (epi == kBEpiNorm) go(std::true_type(), E1());
+            else if (epi == kBEpiUpdate) go(std::true_type(), E2());
+            else go(std::true_type(), E0());
         } else {
-            if (dag) k_batch_hop<true, false, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
-            else k_batch_hop<false, false, S, M><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+            if (epi == kBEpiNorm) go(std::false_type(), E1());
+            else if (epi == kBEpiUpdate) go(std::false_type(), E2());
+            else go(std::false_type(), E0());
         }
         WD_LAUNCHED(ctx_);
         return WD_OK;
@@ -695,50 +761,86 @@ wd_status BatchEngine::hop(int h, int cb, int dag, int v)
     }
 }
 
-wd_status BatchEngine::iteration(const BState &bst)
+wd_status BatchEngine::iteration()
 {
     const int nsys = (int)sys_.size();
     const bool f16 = L_ == WD_PREC_F16;
     const int v = hop_variant_;
     wd_status e;
-    if ((e = hop(0, 1, 0, v)) != WD_OK || (e = hop(1, 0, 0, v)) != WD_OK) return e;  // t = Mhat p
-    if ((e = hop(2, 1, 1, v)) != WD_OK || (e = hop(3, 0, 1, v)) != WD_OK) return e;  // q = Mhat^dag t
-    if (f16) k_batch_norm_t<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
-    else k_batch_norm_t<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    // t = Mhat p with |t|^2 -> alpha
+    if ((e = hop(0, 1, 0, v, kBEpiPlain)) != WD_OK || (e = hop(1, 0, 0, v, kBEpiNorm)) != WD_OK) return e;
+    k_batch_scalars<<<nsys, kScalThreads, 0, ctx_->stream>>>(d_sys_[1].p, d_sc_.p, d_partial_.p, 0, 0.0);
     WD_LAUNCHED(ctx_);
-    k_batch_scalars<<<(nsys + 127) / 128, 128, 0, ctx_->stream>>>(d_vec_.p, bst, nsys, 0);
+    // q = Mhat^dag t applied as the update, |r_s|^2 -> beta (or a reliable update due)
+    if ((e = hop(2, 1, 1, v, kBEpiPlain)) != WD_OK || (e = hop(3, 0, 1, v, kBEpiUpdate)) != WD_OK) return e;
+    k_batch_scalars<<<nsys, kScalThreads, 0, ctx_->stream>>>(d_sys_[3].p, d_sc_.p, d_partial_.p, 1, delta_ * delta_);
     WD_LAUNCHED(ctx_);
-    if (f16) k_batch_update<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
-    else k_batch_update<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
-    WD_LAUNCHED(ctx_);
-    k_batch_scalars<<<(nsys + 127) / 128, 128, 0, ctx_->stream>>>(d_vec_.p, bst, nsys, 1);
-    WD_LAUNCHED(ctx_);
-    if (f16) k_batch_xpay<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
-    else k_batch_xpay<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, bst);
+    if (f16) k_batch_xpay<true><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, d_chunk_sys_.p, d_sc_.p);
+    else k_batch_xpay<false><<<nchunks_, WD_RED_THREADS, 0, ctx_->stream>>>(d_vec_.p, d_chunk_sys_.p, d_sc_.p);
     WD_LAUNCHED(ctx_);
     return WD_OK;
+}
+
+wd_status BatchEngine::rel_streams()
+{
+    if (rel_stream_[0]) return WD_OK;
+    for (auto &q : rel_stream_) WD_CUDA(ctx_, cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
+    for (auto &e : rel_ev_) WD_CUDA(ctx_, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return WD_OK;
+}
+
+// the reliable updates of systems upd, spread over the update streams
+// (each system's kernels in order on one stream, with its own reduction
+// scratch), joined back into the context's stream
+wd_status BatchEngine::reliable_round(const std::vector<int> &upd)
+{
+    const int ns = std::min<int>(kRelStreams, (int)upd.size());
+    if (ns <= 1) {
+        for (int j : upd)
+            if (wd_status st = reliable_enqueue(*sys_[j], false, d_rel_.p + 2 * j, d_rel_.p + 2 * j + 1))
+                return st;
+        return WD_OK;
+    }
+    wd_status st = rel_streams();
+    if (st != WD_OK) return st;
+    cudaStream_t main = ctx_->stream;
+    WD_CUDA(ctx_, cudaEventRecord(rel_ev_[kRelStreams], main));
+    for (int i = 0; i < ns; ++i) WD_CUDA(ctx_, cudaStreamWaitEvent(rel_stream_[i], rel_ev_[kRelStreams], 0));
+    for (size_t u = 0; u < upd.size() && st == WD_OK; ++u) {
+        const int j = upd[u];
+        ctx_->stream = rel_stream_[u % ns];  // every launch of this system's update goes to its stream
+        st = reliable_enqueue(*sys_[j], false, d_rel_.p + 2 * j, d_rel_.p + 2 * j + 1);
+        ctx_->stream = main;
+    }
+    // join every stream that was given work, also after an error
+    for (int i = 0; i < ns; ++i) {
+        cudaEventRecord(rel_ev_[i], rel_stream_[i]);
+        cudaStreamWaitEvent(main, rel_ev_[i], 0);
+    }
+    return st;
 }
 
 wd_status BatchEngine::upload_scalars()
 {
     const int nsys = (int)sys_.size();
-    std::vector<double> rr(nsys);
-    std::vector<int> act(nsys);
+    h_sc_.assign(nsys, BScal{});
     for (int k = 0; k < nsys; ++k) {
-        rr[k] = sys_[k]->rr;
-        act[k] = sys_[k]->active ? 1 : 0;
+        const EngineSys &s = *sys_[k];
+        BScal &c = h_sc_[k];
+        c.rr = s.rr;
+        c.rr_max = s.rr_max;
+        c.target2 = s.target * s.target;
+        c.active = s.active ? 1 : 0;
+        c.wait = 0;
+        c.iters = s.iters;
     }
-    wd_status st;
-    if ((st = d_rr_.put(ctx_, rr)) != WD_OK) return st;
-    if ((st = d_active_.put(ctx_, act)) != WD_OK) return st;
     scalars_dirty_ = false;
-    return WD_OK;
+    return d_sc_.put(ctx_, h_sc_);
 }
 
 wd_status BatchEngine::step(std::vector<int> *finished)
 {
     const auto t0 = std::chrono::steady_clock::now();
-    const size_t before = results.size();
     wd_status st;
     // compact when systems joined or half the tables are masked
     size_t masked = 0;
@@ -748,52 +850,66 @@ wd_status BatchEngine::step(std::vector<int> *finished)
     } else if (scalars_dirty_) {
         if ((st = upload_scalars()) != WD_OK) return st;
     }
-    if (sys_.empty() || !exec_) return WD_OK;
-    WD_CUDA(ctx_, cudaGraphLaunch(exec_, ctx_->stream));
-    ctx_->launches += kernels_per_graph_;
     const int nsys = (int)sys_.size();
-    std::vector<double> rr(nsys);
-    WD_CUDA(ctx_, cudaMemcpyAsync(rr.data(), d_rr_.p, nsys * sizeof(double), cudaMemcpyDeviceToHost, ctx_->stream));
+    if (nsys == 0) return WD_OK;
+    // iterations to queue: the shortest expected remainder of a cycle
+    int k = kMaxPerGraph;
+    for (auto &s : sys_)
+        if (s->active) k = std::min(k, std::max(1, std::min(s->cycle - s->since, max_iter_ - s->iters)));
+    cudaGraphExec_t exec = nullptr;
+    if ((st = graph(k, &exec)) != WD_OK) return st;
+    WD_CUDA(ctx_, cudaGraphLaunch(exec, ctx_->stream));
+    ctx_->launches += kernels_per_iter_ * (uint64_t)k;
+    h_sc_.resize(nsys);
+    WD_CUDA(ctx_, cudaMemcpyAsync(h_sc_.data(), d_sc_.p, nsys * sizeof(BScal), cudaMemcpyDeviceToHost, ctx_->stream));
     WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
-    // systems whose residual fell by delta (or reached the target) take a
-    // reliable update; the updates of up to kRelGroup systems are enqueued
-    // back to back and their norms fetched with one host wait
+    // systems the device masked for a reliable update take it now, all
+    // enqueued back to back with one host wait for their norms
     std::vector<int> upd;
-    for (int k = 0; k < nsys; ++k) {
-        EngineSys &s = *sys_[k];
+    std::vector<double> rr_old(nsys), rr_trig(nsys);
+    for (int j = 0; j < nsys; ++j) {
+        EngineSys &s = *sys_[j];
         if (!s.active) continue;
-        s.iters += per_graph_;
-        const double rr_new = rr[k];
-        if (!std::isfinite(rr_new)) return wd_fail(ctx_, WD_ERR_NAN, "batched CG residual is not finite");
-        s.rr = rr_new;
-        if (rr_new < delta_ * delta_ * s.rr_max || std::sqrt(rr_new) <= s.target) upd.push_back(k);
-        else if (s.iters >= max_iter_ && (st = finish(s)) != WD_OK)  // give up: return what it has
-            return st;
+        const BScal &c = h_sc_[j];
+        s.since += c.iters - s.iters;
+        s.iters = c.iters;
+        if (c.wait == 2) return wd_fail(ctx_, WD_ERR_NAN, "batched CG residual is not finite");
+        if (c.wait == 0) s.rr = c.rr;  // the device's current iterate
+        if (c.wait == 1) {
+            upd.push_back(j);
+            rr_old[j] = c.rr;
+            rr_trig[j] = c.rr_new;
+        } else if (s.iters >= max_iter_) {
+            if ((st = finish(s)) != WD_OK) return st;  // give up: return what it has
+        }
     }
-    for (size_t g0 = 0; g0 < upd.size(); g0 += kRelGroup) {
-        const size_t g1 = std::min(upd.size(), g0 + kRelGroup);
-        for (size_t j = g0; j < g1; ++j)
-            if ((st = reliable_enqueue(*sys_[upd[j]], false, 2 * (int)(j - g0))) != WD_OK) return st;
-        double2 red[2 * kRelGroup];
-        if ((st = wd_red_fetch(ctx_, 2 * (int)(g1 - g0), red)) != WD_OK) return st;
-        for (size_t j = g0; j < g1; ++j) {
-            EngineSys &s = *sys_[upd[j]];
-            const double rrt = red[2 * (j - g0)].x, ss = red[2 * (j - g0) + 1].x;
-            const bool at_target = std::sqrt(s.rr) <= s.target;
+    if (!upd.empty()) {
+        if ((st = reliable_round(upd)) != WD_OK) return st;
+        std::vector<double> rel(2 * (size_t)nsys);
+        WD_CUDA(ctx_, cudaMemcpyAsync(rel.data(), d_rel_.p, rel.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                      ctx_->stream));
+        WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
+        for (int j : upd) {
+            EngineSys &s = *sys_[j];
+            const double rrt = rel[2 * j], ss = rel[2 * j + 1];
             s.updates++;
+            s.cycle = std::max(1, s.since);
+            s.since = 0;
             s.true_res = std::sqrt(ss) / s.norm_b;
             if (s.true_res <= s.tol) {
                 if ((st = finish(s)) != WD_OK) return st;
                 continue;
             }
-            if (at_target) {
+            if (std::sqrt(rr_trig[j]) <= s.target) {
                 s.ratio = ss > 0 ? std::sqrt(rrt / ss) : s.ratio;
                 s.target = std::fmin(s.target * 0.5, s.tol * s.norm_b * s.ratio * 0.5);
             }
-            s.rr = s.rr_max = rrt;  // continue from the recomputed residual
-            scalars_dirty_ = true;
+            // continue from the recomputed residual: p = r_s + (|r_s|^2 / previous |r_s|^2) p
+            if ((st = wd_mx_xpay(ctx_, s.lat->g.Vh, L_, s.B.rs.v, rrt / rr_old[j], s.B.p.v)) != WD_OK) return st;
+            s.rr = s.rr_max = rrt;
             if (s.iters >= max_iter_ && (st = finish(s)) != WD_OK) return st;
         }
+        scalars_dirty_ = true;
     }
     WD_CUDA(ctx_, cudaStreamSynchronize(ctx_->stream));
     solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -801,7 +917,6 @@ wd_status BatchEngine::step(std::vector<int> *finished)
         finished->clear();
         take_retired(finished);
     }
-    (void)before;
     return WD_OK;
 }
 
@@ -825,7 +940,7 @@ extern "C" wd_status wd_solve_batch(wd_context *ctx, int nsys, const wd_lattice 
     }
     const wd_precision H = prm->prec_reliable == WD_PREC_DF64 ? WD_PREC_DF64 : WD_PREC_F64;
     const double delta = prm->delta > 0 && prm->delta < 1 ? prm->delta : 0.1;
-    BatchEngine eng(ctx, prm->prec, H, delta, 4, prm->max_iter);
+    BatchEngine eng(ctx, prm->prec, H, delta, prm->max_iter);
     wd_status st;
     for (int i = 0; i < nsys; ++i)
         if ((st = eng.add(i, lats[i], srcs[i]->d, dests[i]->d, masses[i], prm->tol)) != WD_OK) return st;
@@ -961,7 +1076,7 @@ extern "C" wd_status wd_server_create(wd_context *ctx, const wd_server_config *c
     if (cfg->prec != WD_PREC_F64) {
         const wd_precision H = cfg->prec_reliable == WD_PREC_DF64 ? WD_PREC_DF64 : WD_PREC_F64;
         const double delta = cfg->delta > 0 && cfg->delta < 1 ? cfg->delta : 0.1;
-        sv->eng = std::make_unique<BatchEngine>(ctx, cfg->prec, H, delta, 4, cfg->max_iter);
+        sv->eng = std::make_unique<BatchEngine>(ctx, cfg->prec, H, delta, cfg->max_iter);
     }
     *out = sv;
     return WD_OK;

@@ -27,6 +27,7 @@
 #include "wd_df2.cuh"
 #include "wd_async.cuh"
 #include "wd_kernels.h"
+#include "wd_reduce.cuh"
 #include <type_traits>
 #include "wd_tune.h"
 
@@ -279,15 +280,14 @@ __device__ __forceinline__ void stage_step(const SplitDF &p, const SplitCtx &x, 
     stage_compute<D, DAG>(x, base + (D % NS) * kOps * stride, stride, acc);
 }
 
+// this thread's colour of the hopping sum at its site (staged, packed)
 template <bool DAG, int WARPS, int LOOK, int NS, bool LCG>
-__global__ void __launch_bounds__(32 * WARPS) k_hop_df_staged(const SplitDF p)
+__device__ __forceinline__ void df_staged_site(const SplitDF &p, const SplitCtx &x, dfp *acc)
 {
     static_assert(LOOK >= 1 && NS >= LOOK + 1, "slot count");
     __shared__ float4 slots[NS * kOps * 32 * WARPS];
-    const SplitCtx x = split_ctx<WARPS>(p);
     constexpr int stride = 32 * WARPS;
     float4 *base = slots + threadIdx.x;
-    dfp acc[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfp());
     stage_issue<0, LCG>(p, x, base, stride);
@@ -304,7 +304,53 @@ __global__ void __launch_bounds__(32 * WARPS) k_hop_df_staged(const SplitDF p)
     stage_step<5, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
     stage_step<6, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
     stage_step<7, DAG, LOOK, NS, LCG>(p, x, base, stride, acc);
+}
+
+template <bool DAG, int WARPS, int LOOK, int NS, bool LCG>
+__global__ void __launch_bounds__(32 * WARPS) k_hop_df_staged(const SplitDF p)
+{
+    const SplitCtx x = split_ctx<WARPS>(p);
+    dfp acc[4];
+    df_staged_site<DAG, WARPS, LOOK, NS, LCG>(p, x, acc);
     pair_epilogue(p, x, acc);
+}
+
+// The reliable update's second Schur hop fused with the true residual
+// (wd_hop_hi_residual): s = bhat - (alpha acc + beta x) in double-float,
+// rounded to FP32 into s32 (plane c/2, half c&1 of the float4 for component
+// c), |s32|^2 reduced over the grid into *result.
+struct ResSinkDF {
+    const float4 *bhat;
+    float4 *s32;
+    double *partial;
+    unsigned *counter;
+    double *result;
+};
+
+template <int WARPS, bool LCG>
+__global__ void __launch_bounds__(32 * WARPS) k_hop_df_res(const SplitDF p, const ResSinkDF r)
+{
+    const SplitCtx x = split_ctx<WARPS>(p);
+    dfp acc[4];
+    df_staged_site<false, WARPS, 1, 2, LCG>(p, x, acc);
+    float n = 0.f;
+    if (x.on) {
+        const size_t Vh = p.g.Vh;
+        const dfp al{make_float2(p.alpha.h, p.alpha.h), make_float2(p.alpha.l, p.alpha.l)};
+        const dfp be{make_float2(p.beta.h, p.beta.h), make_float2(p.beta.l, p.beta.l)};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int c = k * 3 + x.col;
+            const size_t i = (size_t)c * Vh + x.s;
+            const dfp o = df_madd2(df_mul2(al, acc[k]), be, dfp_from_f4(p.x[i]));
+            const dfp sd = df_add2(dfp_from_f4(r.bhat[i]), df_neg2(o));
+            const float2 v = make_float2(__fadd_rn(sd.h.x, sd.l.x), __fadd_rn(sd.h.y, sd.l.y));
+            reinterpret_cast<float2 *>(r.s32 + (size_t)(c >> 1) * Vh + x.s)[c & 1] = v;
+            n = fmaf(v.x, v.x, fmaf(v.y, v.y, n));
+        }
+    }
+    double tot;
+    if (wd_grid_sum<32 * WARPS>((double)n, r.partial, r.counter, &tot)) *r.result = tot;
 }
 
 __global__ void k_f64_to_df(const double2 *__restrict__ in, float4 *__restrict__ out, int64_t n)
@@ -387,6 +433,38 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
         if (v == 4) return run_pipe(W4());
         return run_staged(W4(), T());
     });
+}
+
+wd_status wd_hop_df_residual(wd_context *ctx, const wd_lattice *lat, const float4 *in_block, const float4 *x_block,
+                             const float4 *bhat, float4 *s32, double mass, double *partial, unsigned *counter,
+                             double *result)
+{
+    wd_status st = wd_lattice_gauge_df(ctx, lat);
+    if (st != WD_OK) return st;
+    const double a = 4.0 + mass;
+    SplitDF p;
+    p.g = lat->g;
+    p.cb = 0;
+    p.in = in_block;
+    p.gauge = lat->gauge_df;
+    p.x = x_block;
+    p.out = nullptr;
+    p.alpha = df_split(-0.25 / a);
+    p.beta = df_split(a);
+    const ResSinkDF r{bhat, s32, partial, counter, result};
+    auto run = [&](auto warps, auto lcg) -> wd_status {
+        constexpr int W = decltype(warps)::value;
+        const int sites_per_block = kSitesPerWarp * W;
+        const int blocks = (lat->g.Vh + sites_per_block - 1) / sites_per_block;
+        k_hop_df_res<W, decltype(lcg)::value><<<blocks, 32 * W, 0, ctx->stream>>>(p, r);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
+    // the plain double-float hop's tuned shape among the staged variants
+    const int v = wd_tune_choice(ctx, "hop_df64", lat->g.Vh);
+    if (v == 1) return run(std::integral_constant<int, 2>(), std::true_type());
+    if (v == 2) return run(std::integral_constant<int, 2>(), std::false_type());
+    return run(std::integral_constant<int, 4>(), std::true_type());
 }
 
 wd_status wd_convert_f64_to_df(wd_context *ctx, const double2 *in, float4 *out, int64_t n)

@@ -13,6 +13,7 @@
 #include <cstdint>
 #include "wd_hop.cuh"
 #include "wd_kernels.h"
+#include "wd_reduce.cuh"
 #include <type_traits>
 #include "wd_tune.h"
 
@@ -123,7 +124,85 @@ struct HopF64AoS : HopF64<THREADS> {
     }
 };
 
+// The reliable update's second Schur hop fused with the true residual:
+// s = bhat - (alpha acc + beta x), rounded to FP32 into s32 (FP32 site
+// layout: plane j holds components 2j, 2j+1), |s32|^2 reduced over the grid.
+struct ResSink {
+    const double2 *bhat;
+    float4 *s32;
+    double *partial;
+    unsigned *counter;
+    double *result;
+};
+
+template <bool DAG, class P>
+__global__ void __launch_bounds__(P::kThreads) k_hop_f64_res(const P p, const ResSink r)
+{
+    const int s = blockIdx.x * P::kThreads + threadIdx.x;
+    float n = 0.f;
+    if (s < p.g.Vh) {
+        double2 acc[12];
+        wd_hop_site<DAG>(p, s, acc);
+        const size_t Vh = p.g.Vh;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) {
+            float v[4];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const size_t i = (size_t)(2 * j + h) * Vh + s;
+                const double2 o = c_axpby(p.alpha, acc[2 * j + h], p.beta, p.x[i]);
+                const double2 b = r.bhat[i];
+                v[2 * h] = (float)(b.x - o.x);
+                v[2 * h + 1] = (float)(b.y - o.y);
+                n = fmaf(v[2 * h], v[2 * h], fmaf(v[2 * h + 1], v[2 * h + 1], n));
+            }
+            r.s32[(size_t)j * Vh + s] = make_float4(v[0], v[1], v[2], v[3]);
+        }
+    }
+    double tot;
+    if (wd_grid_sum<P::kThreads>((double)n, r.partial, r.counter, &tot)) *r.result = tot;
+}
+
 }  // namespace
+
+wd_status wd_hop_df_residual(wd_context *ctx, const wd_lattice *lat, const float4 *in_block, const float4 *x_block,
+                             const float4 *bhat, float4 *s32, double mass, double *partial, unsigned *counter,
+                             double *result);
+
+wd_status wd_hop_hi_residual(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec x, WdVec bhat, WdVec s32,
+                             double mass, double *partial, unsigned *counter, double *result)
+{
+    if (in.prec != x.prec || in.prec != bhat.prec || s32.prec != WD_PREC_F32)
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "residual hop: in, x, bhat of one storage, s32 FP32");
+    const double a = 4.0 + mass;
+    if (in.prec == WD_PREC_DF64)
+        return wd_hop_df_residual(ctx, lat, (const float4 *)in.p, (const float4 *)x.p, (const float4 *)bhat.p,
+                                  (float4 *)s32.p, mass, partial, counter, result);
+    if (in.prec != WD_PREC_F64) return wd_fail(ctx, WD_ERR_BAD_ARG, "residual hop: FP64 or double-float storage");
+    const ResSink r{(const double2 *)bhat.p, (float4 *)s32.p, partial, counter, result};
+    auto run = [&](auto tag) -> wd_status {
+        using P = HopF64<decltype(tag)::value>;
+        P p;
+        p.g = lat->g;
+        p.cb = 0;
+        p.in = (const double2 *)in.p;
+        p.gauge = lat->gauge;
+        p.x = (const double2 *)x.p;
+        p.out = nullptr;
+        p.alpha = -0.25 / a;
+        p.beta = a;
+        p.scale = F64Scale::make(p.alpha);
+        const int blocks = (lat->g.Vh + P::kThreads - 1) / P::kThreads;
+        k_hop_f64_res<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p, r);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
+    // the plain FP64 hop's tuned shape: 128, 64 or 256 threads per block
+    const int v = wd_tune_choice(ctx, "hop_f64", lat->g.Vh);
+    if (v == 1) return run(std::integral_constant<int, 64>());
+    if (v == 2) return run(std::integral_constant<int, 256>());
+    return run(std::integral_constant<int, 128>());
+}
 
 wd_status wd_hop_f64_aos_range(wd_context *ctx, cudaStream_t stream, const wd_lattice *lat, const double2 *in_aos,
                                double2 *out_aos, const double2 *x_aos, int cb, int dag, double alpha, double beta,

@@ -329,12 +329,16 @@ wd_status wd_spinor_h16_to_ref(wd_context *ctx, const WdGeom &g, WdVec f, double
 // on which block finishes last -- and updates the solver's device scalars.
 namespace {
 
-enum { kEpiNorm = 0, kEpiUpdate = 1 };
+// kEpiNorm / kEpiUpdate: the CG iteration's steps (device scalars in dev);
+// kEpiNormResult: out stored and |out|^2 written to *result
+enum { kEpiNorm = 0, kEpiUpdate = 1, kEpiNormResult = 2 };
 
 template <class Sp, class Lk, int THREADS, int MINB, int EPI>
 struct HopLPRed : HopLP<Sp, Lk, THREADS, MINB> {
     WdMxDev *dev;
     double *partial;
+    unsigned *counter;  // kEpiNormResult
+    double *result;     // kEpiNormResult
     Sp pvec;       // update: p at the output site (x_s += alpha p)
     SpF32 rs, xs;  // update: iterated residual and solution increment
 
@@ -348,7 +352,7 @@ struct HopLPRed : HopLP<Sp, Lk, THREADS, MINB> {
 #pragma unroll
         for (int c = 0; c < 12; ++c) r[c] = c_axpby(this->alpha, acc[c], bx, xv[c]);
         float n = 0.f;
-        if constexpr (EPI == kEpiNorm) {
+        if constexpr (EPI != kEpiUpdate) {
 #pragma unroll
             for (int c = 0; c < 12; ++c) n = fmaf(r[c].x, r[c].x, fmaf(r[c].y, r[c].y, n));
             this->out.store(s, r);
@@ -426,46 +430,22 @@ template <bool DAG, bool STAGED, int EPI, class P>
 __global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_lp_red(const P p)
 {
     constexpr int T = P::kThreads;
-    if (p.dev->stop) return;  // the same value in every block of the launch
+    if (EPI != kEpiNormResult && p.dev->stop) return;  // the same value in every block of the launch
     const int s = blockIdx.x * T + threadIdx.x;
-    const double v = wd_warp_sum((double)red_site<DAG, STAGED, EPI>(p, s));
-    __shared__ double sw[T / 32];
-    __shared__ int last;
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) sw[w] = v;
-    __syncthreads();
-    unsigned *counter = EPI == kEpiNorm ? &p.dev->count_t : &p.dev->count_r;
-    if (threadIdx.x == 0) {
-        double b = 0.0;
-#pragma unroll
-        for (int i = 0; i < T / 32; ++i) b += sw[i];
-        p.partial[blockIdx.x] = b;
-        __threadfence();
-        last = atomicAdd(counter, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    double t = 0.0;
-    for (int i = threadIdx.x; i < (int)gridDim.x; i += T) t += __ldcg(p.partial + i);
-    t = wd_warp_sum(t);
-    __syncthreads();
-    if (l == 0) sw[w] = t;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double tot = 0.0;
-#pragma unroll
-        for (int i = 0; i < T / 32; ++i) tot += sw[i];
-        *counter = 0;
-        if constexpr (EPI == kEpiNorm) mx_fin_norm(p.dev, tot);
-        else mx_fin_update(p.dev, tot);
-    }
+    const float v = red_site<DAG, STAGED, EPI>(p, s);
+    unsigned *counter = EPI == kEpiNorm ? &p.dev->count_t : EPI == kEpiUpdate ? &p.dev->count_r : p.counter;
+    double tot;
+    if (!wd_grid_sum<T>((double)v, p.partial, counter, &tot)) return;
+    if constexpr (EPI == kEpiNorm) mx_fin_norm(p.dev, tot);
+    else if constexpr (EPI == kEpiUpdate) mx_fin_update(p.dev, tot);
+    else *p.result = tot;
 }
 
 // the launch shape the tuner chose for the plain hop of this storage and size
 template <int EPI, class Sp, class Lk>
 wd_status launch_red(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &b, int dag, WdMxDev *dev,
-                     double *partial, Sp pvec, SpF32 rs, SpF32 xs)
+                     double *partial, Sp pvec, SpF32 rs, SpF32 xs, unsigned *counter = nullptr,
+                     double *result = nullptr)
 {
     constexpr bool kF16 = std::is_same_v<Sp, SpF16>;
     int v = wd_tune_choice(ctx, name, b.g.Vh);
@@ -477,6 +457,7 @@ wd_status launch_red(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &b, 
         q.g = b.g, q.cb = b.cb, q.in = b.in, q.out = b.out, q.x = b.x, q.link = b.link;
         q.has_x = true, q.alpha = b.alpha, q.beta = b.beta;
         q.dev = dev, q.partial = partial, q.pvec = pvec, q.rs = rs, q.xs = xs;
+        q.counter = counter, q.result = result;
         const int blocks = (b.g.Vh + TH - 1) / TH;
         if (dag) k_hop_lp_red<true, ST, EPI><<<blocks, TH, 0, ctx->stream>>>(q);
         else k_hop_lp_red<false, ST, EPI><<<blocks, TH, 0, ctx->stream>>>(q);
@@ -549,4 +530,19 @@ wd_status wd_hop_lp_update(wd_context *ctx, const wd_lattice *lat, WdVec in, WdV
 {
     // out is not written by the update epilogue
     return hop_lp_red<kEpiUpdate>(ctx, lat, in, t, t, p, rs, xs, mass, 1, dev, partial);
+}
+
+wd_status wd_hop_f32_norm(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, WdVec x, double mass, int dag,
+                          double *partial, unsigned *counter, double *result)
+{
+    const int Vh = lat->g.Vh;
+    if (in.prec != WD_PREC_F32 || out.prec != WD_PREC_F32 || x.prec != WD_PREC_F32)
+        return wd_fail(ctx, WD_ERR_BAD_ARG, "wd_hop_f32_norm: FP32 operands");
+    wd_status st = wd_lattice_gauge_lp(ctx, lat, WD_PREC_F32);
+    if (st != WD_OK) return st;
+    const LinkF32 lk{(const float4 *)lat->gauge_f32, Vh};
+    const SpF32 none = sp_f32(out, Vh);
+    return launch_red<kEpiNormResult>(ctx, "hop_f32",
+                                      red_base(lat, sp_f32(in, Vh), sp_f32(out, Vh), sp_f32(x, Vh), lk, mass), dag,
+                                      nullptr, partial, none, none, none, counter, result);
 }

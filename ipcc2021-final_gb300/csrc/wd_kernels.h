@@ -82,6 +82,17 @@ wd_status wd_hop_lp_norm(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec
                          WdMxDev *dev, double *partial);
 wd_status wd_hop_lp_update(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec t, WdVec p, WdVec rs, WdVec xs,
                            double mass, WdMxDev *dev, double *partial);
+// The reliable update's reducing steps (even outputs, Schur operator second
+// hops).  partial: at least Vh/16 + 1 doubles; counter: zero at launch (the
+// last block resets it).
+//  * FP32: out = a x - D_eo in / (4a) (D^dag with dag), stored; |out|^2 -> *result
+wd_status wd_hop_f32_norm(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec out, WdVec x, double mass, int dag,
+                          double *partial, unsigned *counter, double *result);
+//  * high precision (FP64 or double-float storage of in, x, bhat): the true
+//    residual s = bhat - (a x - D_eo in / (4a)) of the Schur system, rounded
+//    to FP32 into s32 (FP32 storage), and |s32|^2 -> *result
+wd_status wd_hop_hi_residual(wd_context *ctx, const wd_lattice *lat, WdVec in, WdVec x, WdVec bhat, WdVec s32,
+                             double mass, double *partial, unsigned *counter, double *result);
 // FP64 block [12][Vh] <-> low-precision block; accumulate != 0 adds into out
 wd_status wd_lp_from_f64(wd_context *ctx, int Vh, const double2 *in, WdVec out);
 wd_status wd_lp_to_f64(wd_context *ctx, int Vh, WdVec in, double2 *out, int accumulate);

@@ -289,10 +289,16 @@ wd_status wd_mx_from_h(wd_context *ctx, int Vh, wd_precision L, wd_precision H, 
 // order as the rounding of a high-precision r to FP32, relative to the
 // current residual -- and costs a quarter of a double-float application.
 // scratch_h: one high-precision half-lattice buffer, used as two FP32 ones.
+wd_status wd_mx_xpay(wd_context *ctx, int Vh, wd_precision L, WdVec rs, double beta, WdVec p)
+{
+    return Mixed{ctx, Vh, L, WD_PREC_F64}.xpay(rs, (float)beta, p);
+}
+
 wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
                          const WdMxReliable &v, const WdVec *p_restart, double *rr, double *ss)
 {
-    wd_status e = wd_mx_reliable_enqueue(ctx, lat, mass, L, H, v, p_restart, 0);
+    double2 *res = (double2 *)ctx->red_partial + WD_RED_BLOCKS;
+    wd_status e = wd_mx_reliable_enqueue(ctx, lat, mass, L, H, v, p_restart, &res[0].x, &res[1].x);
     if (e != WD_OK) return e;
     double2 red[2];
     if ((e = wd_red_fetch(ctx, 2, red)) != WD_OK) return e;
@@ -301,8 +307,11 @@ wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd
     return WD_OK;
 }
 
+size_t wd_mx_reliable_scratch_doubles(int Vh) { return (size_t)Vh / 16 + 3; }
+
 wd_status wd_mx_reliable_enqueue(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
-                                 const WdMxReliable &v, const WdVec *p_restart, int slot)
+                                 const WdMxReliable &v, const WdVec *p_restart, double *rr_dev, double *ss_dev,
+                                 double *scratch)
 {
     const int Vh = lat->g.Vh;
     const int64_t nh = (int64_t)12 * Vh;
@@ -311,14 +320,24 @@ wd_status wd_mx_reliable_enqueue(wd_context *ctx, const wd_lattice *lat, double 
     s32.prec = tmp32.prec = WD_PREC_F32;
     s32.p = v.scratch_h.p;
     tmp32.p = (char *)v.scratch_h.p + (size_t)nh * sizeof(float2);
+    // block partials of the two reductions, then their two counters: the
+    // caller's scratch, or a block from the work-buffer cache
+    const size_t nparts = wd_mx_reliable_scratch_doubles(Vh) - 1;
+    DevBlock blk;
     wd_status e;
+    if (!scratch && (e = blk.alloc(ctx, (nparts + 1) * sizeof(double))) != WD_OK) return e;
+    double *partial = scratch ? scratch : (double *)blk.p;
+    unsigned *count = (unsigned *)(partial + nparts);
+    WD_CUDA(ctx, cudaMemsetAsync(count, 0, 2 * sizeof(unsigned), ctx->stream));
     if ((e = mx.accum(v.xs, v.x_e)) != WD_OK) return e;
-    if ((e = wd_apply_Mhat_v(ctx, lat, v.x_e, v.t_h, v.tmp_oh, mass, 0)) != WD_OK) return e;
-    if ((e = wd_v_xpayz(ctx, v.bhat, make_double2(-1.0, 0.0), v.t_h, v.s_e, nh)) != WD_OK) return e;
-    if ((e = mx.to_f32(v.s_e, s32)) != WD_OK) return e;
-    if ((e = wd_apply_Mhat_v(ctx, lat, s32, v.rs, tmp32, mass, 1)) != WD_OK) return e;
-    if ((e = mx.norm2_f32(v.rs, slot)) != WD_OK) return e;
-    if ((e = wd_v_norm2(ctx, v.s_e, nh, slot + 1)) != WD_OK) return e;
+    // s = bhat - Mhat x_e (high precision, rounded to FP32 as stored), |s|^2 -> slot + 1
+    if ((e = wd_hop_v(ctx, lat, v.x_e, v.tmp_oh, nullptr, 1, 0, 1.0, 0.0)) != WD_OK) return e;
+    if ((e = wd_hop_hi_residual(ctx, lat, v.tmp_oh, v.x_e, v.bhat, s32, mass, partial, count, ss_dev)) != WD_OK)
+        return e;
+    // r_s = Mhat^dag s (FP32), |r_s|^2 -> slot
+    if ((e = wd_hop_v(ctx, lat, s32, tmp32, nullptr, 1, 1, 1.0, 0.0)) != WD_OK) return e;
+    if ((e = wd_hop_f32_norm(ctx, lat, tmp32, v.rs, s32, mass, 1, partial, count + 1, rr_dev)) != WD_OK)
+        return e;
     return p_restart ? mx.f32_to(v.rs, *p_restart) : WD_OK;
 }
 
@@ -334,12 +353,12 @@ wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const dou
     wd_status st;
 
     // high-precision vectors: full source and solution, even-parity work blocks
-    WdVecBuf hs, hx, bhat, s_e, r_h, t_h, tmp_oh;
-    WdVecBuf p, t, q, tmp_ol, rs, xs;
-    WdVecBuf *hbufs[] = {&bhat, &s_e, &r_h, &t_h, &tmp_oh};
+    WdVecBuf hs, hx, bhat, r_h, tmp_oh;
+    WdVecBuf p, t, tmp_ol, rs, xs;
+    WdVecBuf *hbufs[] = {&bhat, &r_h, &tmp_oh};
     for (WdVecBuf *b : hbufs)
         if ((st = wd_vec_alloc(ctx, *b, H, nh)) != WD_OK) return st;
-    WdVecBuf *lbufs[] = {&p, &t, &q, &tmp_ol};
+    WdVecBuf *lbufs[] = {&p, &t, &tmp_ol};
     for (WdVecBuf *b : lbufs)
         if ((st = wd_vec_alloc(ctx, *b, prm->prec, nh)) != WD_OK) return st;
     if ((st = wd_vec_alloc(ctx, rs, WD_PREC_F32, nh)) != WD_OK) return st;
@@ -367,7 +386,7 @@ wd_status wd_solve_cg_eo_mixed(wd_context *ctx, const wd_lattice *lat, const dou
 
     // reliable update: x_e += x_s; s = bhat - Mhat x_e; r_s = Mhat^dag s (p <- r_s only on a restart)
     double rr = 0, ss = 0;
-    const WdMxReliable rv{xs.v, x_e, bhat.v, t_h.v, s_e.v, tmp_oh.v, r_h.v, rs.v};
+    const WdMxReliable rv{xs.v, x_e, bhat.v, tmp_oh.v, r_h.v, rs.v};
     auto reliable = [&](bool reset_p) -> wd_status {
         return wd_mx_reliable(ctx, lat, m, prm->prec, H, rv, reset_p ? &p.v : nullptr, &rr, &ss);
     };

@@ -35,19 +35,28 @@ struct WdMxReliable {
     WdVec xs;         // FP32 solution increment (zeroed)
     WdVec x_e;        // high-precision solution
     WdVec bhat;       // high-precision Schur source
-    WdVec t_h, s_e;   // high-precision work; s_e receives the true residual
     WdVec tmp_oh;     // high-precision odd-parity work
     WdVec scratch_h;  // high-precision work, used as two FP32 blocks
     WdVec rs;         // FP32 iterated residual, receives Mhat^dag s
 };
-// x_e += xs; s = bhat - Mhat x_e (high); rs = Mhat^dag s (FP32); rr = |rs|^2,
-// ss = |s|^2; p_restart (storage L) <- rs when given
+// x_e += xs; s = bhat - Mhat x_e (high precision, kept only as FP32);
+// rs = Mhat^dag s (FP32); rr = |rs|^2, ss = |s|^2; p_restart (storage L) <- rs
+// when given
 wd_status wd_mx_reliable(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
                          const WdMxReliable &v, const WdVec *p_restart, double *rr, double *ss);
-// the same with no host wait: |rs|^2 lands in reduction slot `slot`, |s|^2 in
-// slot + 1, for the caller to fetch (several systems per fetch)
+// the same with no host wait: |rs|^2 and |s|^2 land in the device doubles
+// rr_dev and ss_dev, for the caller to fetch (several systems per fetch).
+// Its kernels go to ctx->stream.  scratch (device, optional): the
+// reductions' work space of wd_mx_reliable_scratch_doubles(Vh) doubles,
+// owned by the caller -- needed when updates of several systems run on
+// different streams at once; without it a block from the context's
+// work-buffer cache (stream-ordered on ctx->stream) is used.
 wd_status wd_mx_reliable_enqueue(wd_context *ctx, const wd_lattice *lat, double mass, wd_precision L, wd_precision H,
-                                 const WdMxReliable &v, const WdVec *p_restart, int slot);
+                                 const WdMxReliable &v, const WdVec *p_restart, double *rr_dev, double *ss_dev,
+                                 double *scratch = nullptr);
+size_t wd_mx_reliable_scratch_doubles(int Vh);
+// p (storage L) = rs (FP32) + beta p
+wd_status wd_mx_xpay(wd_context *ctx, int Vh, wd_precision L, WdVec rs, double beta, WdVec p);
 
 // Device-side scalars of one mixed-precision solve.  The iteration kernels
 // read and write them, so iterations run back to back with no host wait: the
