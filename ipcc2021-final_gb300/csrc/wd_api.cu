@@ -520,8 +520,14 @@ static uint64_t gauge_fingerprint(const int dims[4], const double *const gauge[4
     return h;
 }
 
-static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *const gauge[4])
+// *deferred (optional): when the cached lattice was built from the same
+// arrays, the fingerprint check is left to the caller (*deferred = true), to
+// run on the host while the device works (host_pipeline's overlap step);
+// the caller re-checks with host_refresh_if_changed.
+static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *const gauge[4],
+                              bool *deferred = nullptr)
 {
+    if (deferred) *deferred = false;
     if (!ctx || !dims || !gauge) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
     for (int i = 0; i < 4; ++i)
         if (!gauge[i] || dims[i] <= 0) return wd_fail(ctx, WD_ERR_BAD_ARG, "bad gauge pointer or extent");
@@ -529,6 +535,10 @@ static wd_status host_prepare(wd_context *ctx, const int dims[4], const double *
     if (same)
         for (int i = 0; i < 4; ++i)
             same = same && ctx->host_lat->g.L[i] == dims[i] && ctx->host_gauge_ptr[i] == gauge[i];
+    if (same && deferred) {
+        *deferred = true;
+        return WD_OK;
+    }
     const uint64_t print = gauge_fingerprint(dims, gauge);
     if (same && print == ctx->host_gauge_print) return WD_OK;
     if (same) {  // same arrays, new contents: refresh the links only
@@ -576,9 +586,11 @@ static bool host_pageable(const void *p)
     return a.type == cudaMemoryTypeUnregistered;
 }
 
-template <class Compute>
+// overlap() runs on the calling thread once everything is enqueued, while
+// the device works.
+template <class Compute, class Overlap>
 static wd_status host_pipeline(wd_context *ctx, const double *src, double *dest, int in_mask, int out_mask,
-                               Compute compute)
+                               Compute compute, Overlap overlap)
 {
     const wd_lattice *lat = ctx->host_lat;
     const WdGeom &g = lat->g;
@@ -652,6 +664,7 @@ static wd_status host_pipeline(wd_context *ctx, const double *src, double *dest,
         return WD_OK;
     };
     st = enqueue();
+    if (st == WD_OK) overlap();
     // a parity of dest the operator does not write is zero.  Four threads: the
     // copies to and from host memory run meanwhile, and a wider team both
     // competes with them for host memory bandwidth and, on a busy host, waits
@@ -678,19 +691,42 @@ static wd_status host_pipeline(wd_context *ctx, const double *src, double *dest,
 // DslashoffdNew on host arrays: only the source parity the term reads (1-cb)
 // is uploaded, and the other parity of dest -- zero by the reference's
 // semantics, src/dslash_new.cpp:1398 -- is cleared on the host meanwhile.
+// Runs a host-buffer operator with the cached links, checking the links'
+// fingerprint on the host while the device works; if the caller's links
+// changed in place since they were uploaded, they are uploaded again and the
+// operator runs once more on the new links.
+template <class Run>
+static wd_status host_run_checked(wd_context *ctx, const int dims[4], const double *const gauge[4], bool deferred,
+                                  Run run)
+{
+    uint64_t print = 0;
+    wd_status st = run([&] {
+        if (deferred) print = gauge_fingerprint(dims, gauge);
+    });
+    if (st != WD_OK || !deferred || print == ctx->host_gauge_print) return st;
+    if ((st = upload_gauge(ctx, ctx->host_lat, gauge)) != WD_OK) return st;
+    ctx->host_gauge_print = print;
+    return run([] {});
+}
+
 extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], const double *const gauge[4],
                                          const double *src, double *dest, int dag, int cb)
 {
-    wd_status st = host_prepare(ctx, dims, gauge);
+    bool deferred = false;
+    wd_status st = host_prepare(ctx, dims, gauge, &deferred);
     if (st != WD_OK) return st;
     if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
     if (cb != 0 && cb != 1) return wd_fail(ctx, WD_ERR_BAD_ARG, "cb must be 0 or 1");
     const size_t half = (size_t)12 * ctx->host_lat->g.Vh;
-    return host_pipeline(ctx, src, dest, 1 << (1 - cb), 1 << cb,
-                         [&](cudaStream_t cs, int p, int lo, int hi, const double2 *in, double2 *out) {
-                             return wd_hop_f64_aos_range(ctx, cs, ctx->host_lat, in + (1 - p) * half,
-                                                         out + p * half, nullptr, p, dag, -0.5, 0.0, lo, hi);
-                         });
+    return host_run_checked(ctx, dims, gauge, deferred, [&](auto overlap) {
+        return host_pipeline(
+            ctx, src, dest, 1 << (1 - cb), 1 << cb,
+            [&](cudaStream_t cs, int p, int lo, int hi, const double2 *in, double2 *out) {
+                return wd_hop_f64_aos_range(ctx, cs, ctx->host_lat, in + (1 - p) * half, out + p * half, nullptr, p,
+                                            dag, -0.5, 0.0, lo, hi);
+            },
+            overlap);
+    });
 }
 
 // DslashNew / Dslash on host arrays (src/invert.cpp:123-156): both parities go
@@ -699,16 +735,21 @@ extern "C" wd_status wd_host_dslash_offd(wd_context *ctx, const int dims[4], con
 extern "C" wd_status wd_host_dslash_full(wd_context *ctx, const int dims[4], const double *const gauge[4],
                                          const double *src, double *dest, double mass, int dag)
 {
-    wd_status st = host_prepare(ctx, dims, gauge);
+    bool deferred = false;
+    wd_status st = host_prepare(ctx, dims, gauge, &deferred);
     if (st != WD_OK) return st;
     if (!src || !dest) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
     const size_t half = (size_t)12 * ctx->host_lat->g.Vh;
     const double a = 4.0 + mass;
-    return host_pipeline(ctx, src, dest, 3, 3,
-                         [&](cudaStream_t cs, int p, int lo, int hi, const double2 *in, double2 *out) {
-                             return wd_hop_f64_aos_range(ctx, cs, ctx->host_lat, in + (1 - p) * half,
-                                                         out + p * half, in + p * half, p, dag, -0.5, a, lo, hi);
-                         });
+    return host_run_checked(ctx, dims, gauge, deferred, [&](auto overlap) {
+        return host_pipeline(
+            ctx, src, dest, 3, 3,
+            [&](cudaStream_t cs, int p, int lo, int hi, const double2 *in, double2 *out) {
+                return wd_hop_f64_aos_range(ctx, cs, ctx->host_lat, in + (1 - p) * half, out + p * half, in + p * half,
+                                            p, dag, -0.5, a, lo, hi);
+            },
+            overlap);
+    });
 }
 
 extern "C" wd_status wd_host_cg(wd_context *ctx, const int dims[4], const double *const gauge[4],
