@@ -9,6 +9,7 @@
 // arithmetic plus unpacking) at the instruction-issue bound.
 #include "wd_hop.cuh"
 #include "wd_lp_staged.cuh"
+#include "wd_h16m.cuh"
 #include "wd_kernels.h"
 #include "wd_reduce.cuh"
 #include "wd_solver.h"
@@ -160,10 +161,9 @@ wd_status launch_hop(wd_context *ctx, const P &p, int dag)
     return WD_OK;
 }
 
-// the FP16 hopping kernel with the next direction's operands staged in
-// shared memory (wd_lp_staged.cuh)
+// the FP16 kernel with FP16-operand arithmetic (wd_h16m.cuh), staged operands
 template <bool DAG, class P>
-__global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_lp_staged(const P p)
+__global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_h16m(const P p)
 {
     using Sp = decltype(p.in);
     using Lk = decltype(p.link);
@@ -172,36 +172,38 @@ __global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_lp
     const int s = blockIdx.x * P::kThreads + threadIdx.x;
     if (s >= p.g.Vh) return;
     float2 acc[12];
-    lp_hop_site_staged<DAG>(p, s, acc, st);
+    h16_hop_site_staged<DAG>(p, s, acc, st);
     p.epilogue(s, acc);
 }
 
 template <class P>
-wd_status launch_hop_staged(wd_context *ctx, const P &p, int dag)
+wd_status launch_hop_h16m(wd_context *ctx, const P &p, int dag)
 {
     const int blocks = (p.g.Vh + P::kThreads - 1) / P::kThreads;
-    if (dag) k_hop_lp_staged<true><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
-    else k_hop_lp_staged<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+    if (dag) k_hop_h16m<true><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
+    else k_hop_h16m<false><<<blocks, P::kThreads, 0, ctx->stream>>>(p);
     WD_LAUNCHED(ctx);
     return WD_OK;
 }
 
-// the same operands in the launch variants the tuner times: 128, 64 or 256
-// threads per block, 128 with registers capped for 8 blocks per SM, and for
-// FP16 the staged kernel with 128 or 64 threads (registers capped at 80).
-// GB300, D_eo at 32^3x64 in us: FP16 74.8 / 75.7 / 79.9 / 73.8 / 71.7 /
-// 71.8 (staged at 48^3x96: 331 against 352); FP32 all within 1 % of 102.5.
+// The launch variants the tuner times.  FP32: 128, 64 or 256 threads per
+// block, or 128 with registers capped for 8 blocks per SM (GB300, D_eo at
+// 32^3x64: all within 1 % of 102.5 us).  FP16: the FP16-operand kernel
+// (wd_h16m.cuh) with each thread's next-direction operands staged in shared
+// memory by cp.async, 128 threads (6 blocks per SM) or 64 (12), registers
+// capped at 80: 63.8 / 63.8 us at 32^3x64, 0.291 / 0.293 ms at 48^3x96.
+// Replaced: the FP16 kernels converting every operand to FP32 first (staged
+// 71.8 us, register-loading 73.8-79.9 us at 32^3x64; 0.331 ms at 48^3x96).
 // Dropped: the staged FP32 kernel (103.1-104.0: 144 bytes per thread and
 // slot leave less L1 for the neighbour spinors), the staged FP16 kernel
-// without the register cap (92-94 registers, 73.7), and a software-pipelined
-// form issuing the next direction's register loads before the current
-// direction's arithmetic (76.1 and 102.4: the compiler already hoists those
-// loads).
+// without the register cap, and a software-pipelined form issuing the next
+// direction's register loads before the current direction's arithmetic (the
+// compiler already hoists those loads).
 template <class Sp, class Lk>
 wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p, int dag)
 {
     constexpr bool kF16 = std::is_same_v<Sp, SpF16>;
-    return wd_tune_launch(ctx, name, p.g.Vh, kF16 ? 6 : 4, [&](int v) -> wd_status {
+    return wd_tune_launch(ctx, name, p.g.Vh, kF16 ? 2 : 4, [&](int v) -> wd_status {
         auto make = [&](auto threads, auto minb) {
             HopLP<Sp, Lk, decltype(threads)::value, decltype(minb)::value> q;
             q.g = p.g, q.cb = p.cb, q.in = p.in, q.out = p.out, q.x = p.x, q.link = p.link;
@@ -212,14 +214,15 @@ wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p
         using T64 = std::integral_constant<int, 64>;
         using T128 = std::integral_constant<int, 128>;
         if constexpr (kF16) {
-            if (v == 4) return launch_hop_staged(ctx, make(T128(), std::integral_constant<int, 6>()), dag);
-            if (v == 5) return launch_hop_staged(ctx, make(T64(), std::integral_constant<int, 12>()), dag);
-        }
-        switch (v) {
-        case 1: return launch_hop(ctx, make(T64(), I0()), dag);
-        case 2: return launch_hop(ctx, make(std::integral_constant<int, 256>(), I0()), dag);
-        case 3: return launch_hop(ctx, make(T128(), std::integral_constant<int, 8>()), dag);
-        default: return launch_hop(ctx, make(T128(), I0()), dag);
+            if (v == 1) return launch_hop_h16m(ctx, make(T64(), std::integral_constant<int, 12>()), dag);
+            return launch_hop_h16m(ctx, make(T128(), std::integral_constant<int, 6>()), dag);
+        } else {
+            switch (v) {
+            case 1: return launch_hop(ctx, make(T64(), I0()), dag);
+            case 2: return launch_hop(ctx, make(std::integral_constant<int, 256>(), I0()), dag);
+            case 3: return launch_hop(ctx, make(T128(), std::integral_constant<int, 8>()), dag);
+            default: return launch_hop(ctx, make(T128(), I0()), dag);
+            }
         }
     });
 }
@@ -403,6 +406,8 @@ __device__ __forceinline__ void mx_fin_update(WdMxDev *d, double rr_new)
     d->rr = rr_new;
 }
 
+// STAGED: the FP16 kernel's staged operands and FP16-operand arithmetic
+// (wd_h16m.cuh); otherwise the register-loading FP32 kernel
 template <bool DAG, bool STAGED, int EPI, class P>
 __device__ __forceinline__ float red_site(const P &p, int s)
 {
@@ -413,7 +418,7 @@ __device__ __forceinline__ float red_site(const P &p, int s)
         __shared__ LpStage<Sp, Lk, P::kThreads> st;
         if (s < p.g.Vh) {
             float2 acc[12];
-            lp_hop_site_staged<DAG>(p, s, acc, st);
+            h16_hop_site_staged<DAG>(p, s, acc, st);
             v = p.epilogue_red(s, acc);
         }
     } else {
@@ -470,13 +475,14 @@ wd_status launch_red(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &b, 
     using Yes = std::true_type;
     using No = std::false_type;
     if constexpr (kF16) {
-        if (v == 4) return run(T128(), std::integral_constant<int, 6>(), Yes());
-        if (v == 5) return run(T64(), std::integral_constant<int, 12>(), Yes());
-    }
-    switch (v) {
-    case 1: return run(T64(), I0(), No());
-    case 2: return run(std::integral_constant<int, 256>(), I0(), No());
-    default: return run(T128(), I0(), No());
+        if (v == 1) return run(T64(), std::integral_constant<int, 12>(), Yes());
+        return run(T128(), std::integral_constant<int, 6>(), Yes());
+    } else {
+        switch (v) {
+        case 1: return run(T64(), I0(), No());
+        case 2: return run(std::integral_constant<int, 256>(), I0(), No());
+        default: return run(T128(), I0(), No());
+        }
     }
 }
 

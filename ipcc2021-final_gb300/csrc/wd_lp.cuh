@@ -90,7 +90,7 @@ struct SpF16 {
         scale[s] = m;
     }
     // shared-memory slot of T threads for the staged kernel (cp.async):
-    // stage() copies site s for thread t, unstage() decodes it as load_raw()
+    // stage() copies site s for thread t (raw halves and the scale)
     template <int T>
     struct Slot {
         uint4 v[3][T];
@@ -102,14 +102,6 @@ struct SpF16 {
 #pragma unroll
         for (int j = 0; j < 3; ++j) wd_cp_async_ca<16>(&S.v[j][t], p + (size_t)j * Vh + s);
         wd_cp_async_ca<4>(&S.sc[t], scale + s);
-    }
-    // unscaled components (as load_raw); returns the site's scale
-    template <int T>
-    __device__ __forceinline__ float unstage(const Slot<T> &S, int t, float2 *v) const
-    {
-#pragma unroll
-        for (int j = 0; j < 3; ++j) unpack4(S.v[j][t], v + 4 * j);
-        return S.sc[t];
     }
 };
 
@@ -172,14 +164,5 @@ struct LinkF16 {
         const size_t i = (size_t)(mu * 2 + par) * Vh + s;
         wd_cp_async_cg16(&S.a[t], a + i);
         wd_cp_async_ca<8>(&S.b[t], b + i);
-    }
-    template <int T>
-    __device__ __forceinline__ void unstage(const Slot<T> &S, int t, float2 *U) const
-    {
-        unpack4(S.a[t], U);
-        const uint2 v = S.b[t];
-        U[4] = h2f(*reinterpret_cast<const __half2 *>(&v.x));
-        U[5] = h2f(*reinterpret_cast<const __half2 *>(&v.y));
-        su3_row2(U);
     }
 };
