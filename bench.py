@@ -379,8 +379,9 @@ def batch_bench(wd, ctx, profile: bool = False) -> dict:
     srcs += [wd.gen_source(dims, 1000 + k) for k in range(12)]
     systems = [(lat, lat.field(b), lat.field(), 0.05) for b in srcs]
     res = {}
-    for name, rel in (("f32_inner_f64_reliable", wd.F64), ("f32_inner_df64_reliable", wd.DF64)):
-        p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=rel)
+    for name, prec, rel in (("f32_inner_f64_reliable", wd.F32, wd.F64), ("f32_inner_df64_reliable", wd.F32, wd.DF64),
+                            ("f16_inner_df64_reliable", wd.F16, wd.DF64)):
+        p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=prec, prec_reliable=rel)
         run(systems, p)  # warm-up
         dt, stats = run(systems, p, timed=True)
         res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt,
@@ -405,8 +406,9 @@ def batch_bench(wd, ctx, profile: bool = False) -> dict:
         lats.append(la)
         systems.append((la, la.field(wd.gen_source(d, 300 + i)), la.field(), float(rng.uniform(0.05, 0.2))))
     res = {}
-    for name, rel in (("batched", wd.F64), ("batched_df64_reliable", wd.DF64)):
-        p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=wd.F32, prec_reliable=rel)
+    for name, prec, rel in (("batched", wd.F32, wd.F64), ("batched_df64_reliable", wd.F32, wd.DF64),
+                            ("batched_f16_inner_df64_reliable", wd.F16, wd.DF64)):
+        p = wd.solver_params(kind=wd.CG_EO, tol=1e-10, max_iter=5000, prec=prec, prec_reliable=rel)
         run(systems, p)
         dt, stats = run(systems, p, timed=True)
         res[name] = {"seconds": dt, "solves_per_s": len(systems) / dt,
@@ -496,13 +498,14 @@ def serve_bench(wd, ctx, n: int, rates_mixed, rates_f64, n_f64: int | None = Non
     out = {"workload": f"{n} Poisson-arrival requests ({len(reqs64)} for plain FP64), sizes "
                        "{8^3x16:.4, 16^3x32:.3, 24^3x48:.2, 32^3x64:.1}, mass U[0.02,0.2], tol {1e-8,1e-10}, "
                        "1-12 sources, 8 resident gauge fields, 150 GB budget",
-           "mixed_batched_f32": [serve_run(wd, ctx, reqs, r, wd.F32) for r in rates_mixed],
-           "plain_f64": [serve_run(wd, ctx, reqs64, r, wd.F64) for r in rates_f64]}
+           "mixed_batched": [serve_run(wd, ctx, reqs, r, wd.F16) for r in rates_mixed],
+           "plain_f64": [serve_run(wd, ctx, reqs64, r, wd.F64) for r in rates_f64],
+           "mixed_batched_solver": "FP16 inner (per-site scale, 12-real links), double-float reliable updates"}
     sat = {k: max((r["solves_per_s"] for r in out[k] if r["saturated"]), default=None)
-           for k in ("mixed_batched_f32", "plain_f64")}
+           for k in ("mixed_batched", "plain_f64")}
     out["saturated_solves_per_s"] = sat
-    if sat["mixed_batched_f32"] and sat["plain_f64"]:
-        out["saturated_ratio_mixed_vs_f64"] = sat["mixed_batched_f32"] / sat["plain_f64"]
+    if sat["mixed_batched"] and sat["plain_f64"]:
+        out["saturated_ratio_mixed_vs_f64"] = sat["mixed_batched"] / sat["plain_f64"]
     return out
 
 

@@ -193,6 +193,8 @@ typedef struct wd_server_config {
     int max_iter;
     double delta;               /* reliable-update threshold (0 -> 0.1) */
 } wd_server_config;
+/* defaults: FP16 inner solver (the fastest), double-float reliable updates, 150 GB budget,
+ * 256 systems, 5000 iterations, delta 0.1 */
 void wd_server_config_default(wd_server_config *c);
 wd_status wd_server_create(wd_context *ctx, const wd_server_config *cfg, wd_server **server);
 void wd_server_destroy(wd_server *server);

@@ -31,6 +31,7 @@
 #include "wd_df.cuh"
 #include "wd_hop.cuh"
 #include "wd_lp.cuh"
+#include "wd_h16m.cuh"
 #include "wd_reduce.cuh"
 #include "wd_solver.h"
 #include "wd_tune.h"
@@ -217,7 +218,9 @@ __global__ void __launch_bounds__(kSites * SYS, MINB) k_batch_hop(const BTable t
     float v = 0.f;
     if (s < G.g.Vh) {
         float2 acc[12];
-        wd_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
+        // FP16 storage: the FP16-operand arithmetic of the solo FP16 kernel
+        if constexpr (F16) h16_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
+        else wd_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
         v = batch_epilogue<F16, EPI>(t, S, sys, s, G.g.Vh, acc);
     }
     if constexpr (EPI != kBEpiPlain) {
@@ -1055,7 +1058,7 @@ static double request_bytes(const wd_server *sv, const wd_lattice *lat, int nsrc
 extern "C" void wd_server_config_default(wd_server_config *c)
 {
     if (!c) return;
-    c->prec = WD_PREC_F32;
+    c->prec = WD_PREC_F16;
     c->prec_reliable = WD_PREC_DF64;
     c->hbm_budget_bytes = 150e9;
     c->max_systems = 256;
