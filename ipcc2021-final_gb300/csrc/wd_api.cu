@@ -600,11 +600,26 @@ static wd_status host_pipeline(wd_context *ctx, const double *src, double *dest,
     wd_status st = ensure_staging(ctx, 4 * half * sizeof(double2));
     if (st != WD_OK) return st;
     double2 *in_aos = (double2 *)ctx->staging, *out_aos = in_aos + 2 * half;
-    // compute chunks of at least 64k sites (at most WD_MAX_CHUNKS); upload units
+    // compute chunks of about 64k sites (at most WD_MAX_CHUNKS); upload units.
+    // The chunk computed first (1) and the one computed last (0) are a
+    // quarter of the others, and chunk 2 half: the first kernel then waits
+    // only for a few slices to arrive, and the last download after the final
+    // kernel is short (pipeline fill and drain).
     int n = std::min(std::min(WD_MAX_CHUNKS, Lt), Vh / 65536);
     if (n < 3) n = 1;
+    int sz[WD_MAX_CHUNKS];
+    if (n >= 4 && Lt >= 2 * n) {
+        const int small = std::max(1, Lt / (4 * n));
+        sz[0] = sz[1] = small;
+        sz[2] = 2 * small;
+        const int rest = Lt - 4 * small, m = n - 3;
+        for (int k = 3; k < n; ++k) sz[k] = rest / m + (k - 3 < rest % m ? 1 : 0);
+    } else {
+        for (int k = 0; k < n; ++k) sz[k] = (int)((int64_t)(k + 1) * Lt / n - (int64_t)k * Lt / n);
+    }
     int tb[WD_MAX_CHUNKS + 1];
-    for (int k = 0; k <= n; ++k) tb[k] = (int)((int64_t)k * Lt / n);
+    tb[0] = 0;
+    for (int k = 0; k < n; ++k) tb[k + 1] = tb[k] + sz[k];
     const int us = n == 1 ? Lt : (Lt + WD_MAX_UPLOADS - 1) / WD_MAX_UPLOADS;  // slices per upload unit
     const int nu = (Lt + us - 1) / us;  // upload units (<= WD_MAX_UPLOADS), unit u = slices [u*us, (u+1)*us)
     // Pageable host buffers: a copy from or to them through the copy engines
