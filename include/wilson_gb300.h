@@ -65,6 +65,12 @@ wd_status wd_context_sync(wd_context *ctx);
 void *wd_context_stream(wd_context *ctx);
 /* Device kernels launched on this context since creation (bookkeeping for benchmarks). */
 uint64_t wd_context_launches(const wd_context *ctx);
+/* Wait for the context's stream, then report (and clear) the device-side
+ * error flag: WD_ERR_CUDA if a kernel's bounded wait gave up since the last
+ * check (the TMA-staged FP16 hopping kernel waits on its copies with an
+ * iteration limit, after which the block writes nothing and sets the flag;
+ * its output is then undefined), else WD_OK. */
+wd_status wd_context_device_check(wd_context *ctx);
 /* Testing aid, host-side failure injection: after n more successful field or
  * work-buffer allocations on this context, the next ones fail with
  * WD_ERR_OOM; n < 0 turns it off (the default).  Returns the previous

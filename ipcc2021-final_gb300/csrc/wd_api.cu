@@ -73,6 +73,8 @@ extern "C" wd_status wd_context_create(int device, wd_context **out)
         e = cudaMalloc(&ctx->red_partial, sizeof(double2) * (WD_RED_BLOCKS + WD_RED_SLOTS));
     if (e == cudaSuccess) e = cudaHostAlloc(&ctx->red_result, sizeof(double2) * WD_RED_SLOTS, 0);
     if (e == cudaSuccess) e = cudaHostAlloc(&ctx->state_host, WD_STATE_HOST_BYTES, 0);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->dev_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->dev_err, 0, sizeof(int));
     if (e != cudaSuccess) {
         wd_context_destroy(ctx);
         cudaGetLastError();
@@ -146,6 +148,7 @@ extern "C" void wd_context_destroy(wd_context *ctx)
     ctx->pool_used.clear();
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     cudaFree(ctx->red_partial);
+    cudaFree(ctx->dev_err);
     cudaFree(ctx->staging);
     if (ctx->red_result) cudaFreeHost(ctx->red_result);
     if (ctx->state_host) cudaFreeHost(ctx->state_host);
@@ -168,6 +171,17 @@ extern "C" wd_status wd_context_sync(wd_context *ctx)
 }
 
 extern "C" void *wd_context_stream(wd_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" wd_status wd_context_device_check(wd_context *ctx)
+{
+    if (!ctx) return WD_ERR_BAD_ARG;
+    int flag = 0;
+    WD_CUDA(ctx, cudaMemcpyAsync(&flag, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (!flag) return WD_OK;
+    WD_CUDA(ctx, cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
+    return wd_fail(ctx, WD_ERR_CUDA, "a kernel's bounded wait gave up (TMA copies did not complete)");
+}
 
 extern "C" int wd_debug_fail_allocations_after(wd_context *ctx, int n)
 {

@@ -7,9 +7,12 @@
 // 1320 flop/site (+ 8 x 66 for the row-2 rebuild) is far below the FP32
 // ridge: FP32 runs at the HBM bound, FP16 (half the bytes, the same
 // arithmetic plus unpacking) at the instruction-issue bound.
+#include <cudaTypedefs.h>
+#include <algorithm>
 #include "wd_hop.cuh"
 #include "wd_lp_staged.cuh"
 #include "wd_h16m.cuh"
+#include "wd_h16_tma.cuh"
 #include "wd_kernels.h"
 #include "wd_reduce.cuh"
 #include "wd_solver.h"
@@ -186,24 +189,181 @@ wd_status launch_hop_h16m(wd_context *ctx, const P &p, int dag)
     return WD_OK;
 }
 
+// ----------------------------------------------------------------------
+// TMA-staged FP16 kernel (wd_h16_tma.cuh): tensor maps and launch.
+
+// cuTensorMapEncodeTiled from the driver, through the runtime's entry-point
+// query (no link against libcuda); null if the driver does not offer it
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder()
+{
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }();
+    return fn;
+}
+
+// a map of 32-bit words: dims innermost first, strides (bytes) of dims 1.., box
+template <int R>
+bool tma_map(CUtensorMap *m, const void *base, const cuuint64_t (&dims)[R], const cuuint64_t (&strides)[R - 1],
+             const cuuint32_t (&box)[R])
+{
+    const auto fn = tma_encoder();
+    if (!fn || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
+    const cuuint32_t unit[5] = {1, 1, 1, 1, 1};  // element strides: every element
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, R, const_cast<void *>(base), dims, strides, box, unit,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+constexpr unsigned kTmaSmemMax = 232448;  // 227 KB: the largest dynamic shared memory of one block
+
+// The maps and shared-memory layout of a BY x BZ tile.  False when the
+// lattice or the operands do not fit the kernel's rules: Lxh a multiple of 4
+// (16-byte scale rows) and at most 32, Ly and Lz multiples of the tile, at
+// most 256 threads (sites) a tile, 16-byte aligned planes.
+bool h16_tma_build(H16TmaMaps &M, const WdGeom &g, const SpF16 &in, int BY, int BZ)
+{
+    const cuuint64_t X = g.Lxh, Ly = g.L[1], Lz = g.L[2], Lt = g.L[3], Vh = g.Vh;
+    if (X % 4 || X > 32 || Ly % BY || Lz % BZ || BY * BZ * X > 256) return false;
+    const cuuint32_t x = (cuuint32_t)X, by = BY, bz = BZ;
+    // spinor planes: words [3][Lt][Lz][Ly][4X]; scales [Lt][Lz][Ly][X]
+    const cuuint64_t sd[5] = {4 * X, Ly, Lz, Lt, 3}, ss[4] = {16 * X, 16 * X * Ly, 16 * X * Ly * Lz, 16 * Vh};
+    const cuuint64_t cd[4] = {X, Ly, Lz, Lt}, cs[3] = {4 * X, 4 * X * Ly, 4 * X * Ly * Lz};
+    const cuuint32_t sbox[3][5] = {{4 * x, by, bz, 1, 3}, {4 * x, 1, bz, 1, 3}, {4 * x, by, 1, 1, 3}};
+    const cuuint32_t cbox[3][4] = {{x, by, bz, 1}, {x, 1, bz, 1}, {x, by, 1, 1}};
+    for (int k = 0; k < 3; ++k) {
+        if (!tma_map<5>(&M.sp[k], in.p, sd, ss, sbox[k])) return false;
+        if (!tma_map<4>(&M.sc[k], in.scale, cd, cs, cbox[k])) return false;
+    }
+    // regions: spinor planes (48 B a site) and scales (4 B) of the tile and
+    // the faces; copy group of region r: (r + 1) / 2
+    const unsigned RC = BY * BZ, rows[7] = {RC, (unsigned)BZ, (unsigned)BZ, (unsigned)BY, (unsigned)BY, RC, RC};
+    unsigned off = 0;
+    for (int k = 0; k < 4; ++k) M.tx_bytes[k] = 0;
+    for (int r = 0; r < 7; ++r) {
+        const unsigned sp = 48 * rows[r] * x, sc = 4 * rows[r] * x;
+        M.off[r] = off;
+        off += (sp + 127) & ~127u;
+        M.off[kRegSc + r] = off;
+        off += (sc + 127) & ~127u;
+        M.tx_bytes[(r + 1) / 2] += sp + sc;
+    }
+    M.stage_bytes = off;
+    return true;
+}
+
+// dynamic shared memory of a launch: the regions, four barriers, alignment slack
+inline unsigned h16_tma_smem(const H16TmaMaps &m) { return m.stage_bytes + 32 + 128; }
+
+// Tensor maps depend only on the spinor's addresses, the geometry and the
+// tile: a small per-thread cache spares re-encoding them at every launch.
+struct TmaKey {
+    const void *in, *scale;
+    int L[4], BY, BZ;
+    bool operator==(const TmaKey &o) const
+    {
+        return in == o.in && scale == o.scale && L[0] == o.L[0] && L[1] == o.L[1] && L[2] == o.L[2] &&
+               L[3] == o.L[3] && BY == o.BY && BZ == o.BZ;
+    }
+};
+
+const H16TmaMaps *h16_tma_maps(const WdGeom &g, const SpF16 &in, int BY, int BZ)
+{
+    struct Entry {
+        TmaKey key;
+        bool ok;
+        H16TmaMaps maps;
+    };
+    thread_local Entry cache[8];
+    thread_local int used = 0, next = 0;
+    const TmaKey key{in.p, in.scale, {g.L[0], g.L[1], g.L[2], g.L[3]}, BY, BZ};
+    for (int i = 0; i < used; ++i)
+        if (cache[i].key == key) return cache[i].ok ? &cache[i].maps : nullptr;
+    Entry &e = cache[next];
+    next = (next + 1) % 8;
+    used = used < 8 ? used + 1 : 8;
+    e.key = key;
+    e.ok = h16_tma_build(e.maps, g, in, BY, BZ);
+    return e.ok ? &e.maps : nullptr;
+}
+
+template <bool DAG, int BY, int BZ, class P>
+void launch_h16_tma_k(wd_context *ctx, const H16TmaArgs<P> &a, int blocks, int threads, unsigned smem)
+{
+    auto k = k_hop_h16_tma<DAG, BY, BZ, P>;
+    static unsigned attr_set = 0;  // devices on which the shared-memory limit is raised
+    if (ctx->device < 32 && !(attr_set & (1u << ctx->device))) {
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmemMax);
+        attr_set |= 1u << ctx->device;
+    }
+    k<<<blocks, threads, smem, ctx->stream>>>(a);
+}
+
+// The TMA-staged FP16 kernel (spinors staged, links loaded per thread), one
+// block per tile; returns false (nothing launched) when the lattice or the
+// operands do not fit it.  Tile: 4 x 4 rows up to Lxh = 16, 4 x 2 beyond.
+template <class P>
+bool launch_hop_h16_tma(wd_context *ctx, const P &p, int dag, wd_status *st)
+{
+    const WdGeom &g = p.g;
+    const int BY = 4, BZ = g.Lxh <= 16 ? 4 : 2;
+    const H16TmaMaps *m = h16_tma_maps(g, p.in, BY, BZ);
+    if (!m || h16_tma_smem(*m) > kTmaSmemMax) return false;
+    H16TmaArgs<HopLP<SpF16, LinkF16>> a;
+    a.m = *m;
+    auto &q = a.p;
+    q.g = p.g, q.cb = p.cb, q.in = p.in, q.out = p.out, q.x = p.x, q.link = p.link;
+    q.has_x = p.has_x, q.alpha = p.alpha, q.beta = p.beta, q.stop = p.stop;
+    a.err = ctx->dev_err;
+    const int threads = BY * BZ * g.Lxh, blocks = g.Vh / threads;
+    const unsigned smem = h16_tma_smem(*m);
+    using A = HopLP<SpF16, LinkF16>;
+    if (BZ == 4) {
+        if (dag) launch_h16_tma_k<true, 4, 4, A>(ctx, a, blocks, threads, smem);
+        else launch_h16_tma_k<false, 4, 4, A>(ctx, a, blocks, threads, smem);
+    } else {
+        if (dag) launch_h16_tma_k<true, 4, 2, A>(ctx, a, blocks, threads, smem);
+        else launch_h16_tma_k<false, 4, 2, A>(ctx, a, blocks, threads, smem);
+    }
+    ctx->launches++;
+    const cudaError_t e = cudaGetLastError();
+    *st = e == cudaSuccess ? WD_OK : wd_cuda_check(ctx, e, "k_hop_h16_tma launch");
+    return true;
+}
+
 // The launch variants the tuner times.  FP32: 128, 64 or 256 threads per
 // block, or 128 with registers capped for 8 blocks per SM (GB300, D_eo at
 // 32^3x64: all within 1 % of 102.5 us).  FP16: the FP16-operand kernel
 // (wd_h16m.cuh) with each thread's next-direction operands staged in shared
 // memory by cp.async, 128 threads (6 blocks per SM) or 64 (12), registers
-// capped at 80: 63.8 / 63.8 us at 32^3x64, 0.291 / 0.293 ms at 48^3x96.
+// capped at 80: 63.8 / 63.8 us at 32^3x64, 0.291 / 0.293 ms at 48^3x96; or
+// the TMA-staged kernel (wd_h16_tma.cuh; 75.8 us and 0.358 ms: every block
+// stalls on its copies before its first direction, and at 3 blocks of 256
+// threads an SM that start-up is not hidden -- issue slots busy 64 % against
+// 74 % for the cp.async kernel).
 // Replaced: the FP16 kernels converting every operand to FP32 first (staged
 // 71.8 us, register-loading 73.8-79.9 us at 32^3x64; 0.331 ms at 48^3x96).
 // Dropped: the staged FP32 kernel (103.1-104.0: 144 bytes per thread and
 // slot leave less L1 for the neighbour spinors), the staged FP16 kernel
-// without the register cap, and a software-pipelined form issuing the next
+// without the register cap, a software-pipelined form issuing the next
 // direction's register loads before the current direction's arithmetic (the
-// compiler already hoists those loads).
+// compiler already hoists those loads), and TMA forms staging the links too
+// (82.0 us: links have no reuse, and the extra 58 KB a tile leave 2 blocks an
+// SM), walking tiles with double buffering (76.0 us, 2 blocks an SM), with
+// 2 x 2 row tiles (75.9 us) or with one barrier for all copies (71.8-73.8 us).
 template <class Sp, class Lk>
 wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p, int dag)
 {
     constexpr bool kF16 = std::is_same_v<Sp, SpF16>;
-    return wd_tune_launch(ctx, name, p.g.Vh, kF16 ? 2 : 4, [&](int v) -> wd_status {
+    return wd_tune_launch(ctx, name, p.g.Vh, kF16 ? 3 : 4, [&](int v) -> wd_status {
         auto make = [&](auto threads, auto minb) {
             HopLP<Sp, Lk, decltype(threads)::value, decltype(minb)::value> q;
             q.g = p.g, q.cb = p.cb, q.in = p.in, q.out = p.out, q.x = p.x, q.link = p.link;
@@ -214,6 +374,11 @@ wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p
         using T64 = std::integral_constant<int, 64>;
         using T128 = std::integral_constant<int, 128>;
         if constexpr (kF16) {
+            if (v == 2) {  // TMA-staged neighbour spinors
+                wd_status st;
+                if (launch_hop_h16_tma(ctx, p, dag, &st)) return st;
+                v = 0;  // the lattice does not fit the TMA kernel
+            }
             if (v == 1) return launch_hop_h16m(ctx, make(T64(), std::integral_constant<int, 12>()), dag);
             return launch_hop_h16m(ctx, make(T128(), std::integral_constant<int, 6>()), dag);
         } else {

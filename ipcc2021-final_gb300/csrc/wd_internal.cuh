@@ -48,6 +48,7 @@ struct wd_context {
     void *red_partial = nullptr;  // WD_RED_BLOCKS double2 (+ result slots)
     void *red_result = nullptr;   // pinned host mirror of the reduction results
     void *state_host = nullptr;   // pinned host mirror of a solver's device scalars (WD_STATE_HOST_BYTES)
+    int *dev_err = nullptr;       // device flag: a kernel's bounded wait gave up (wd_context_device_check)
     void *staging = nullptr;      // device staging buffer for reference-layout copies
     size_t staging_bytes = 0;
     // cached host-buffer path state (wd_host_*): one lattice + fields

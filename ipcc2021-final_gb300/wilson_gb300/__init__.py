@@ -73,6 +73,7 @@ def _load() -> C.CDLL:
         "wd_context_sync": (C.c_int, [vp]),
         "wd_context_stream": (vp, [vp]),
         "wd_context_launches": (C.c_uint64, [vp]),
+        "wd_context_device_check": (C.c_int, [vp]),
         "wd_debug_fail_allocations_after": (C.c_int, [vp, C.c_int]),
         "wd_lattice_create": (C.c_int, [vp, ip, d4, C.POINTER(vp)]),
         "wd_lattice_update": (C.c_int, [vp, vp, d4]),
@@ -255,6 +256,10 @@ class Context:
     @property
     def launches(self) -> int:
         return int(lib.wd_context_launches(self.handle))
+
+    def device_check(self) -> None:
+        """Wait for the stream and raise if a kernel's bounded wait gave up."""
+        self.check(lib.wd_context_device_check(self.handle))
 
     def fail_allocations_after(self, n: int) -> int:
         """Testing aid: the next allocations after n more successful ones fail
