@@ -15,11 +15,15 @@
 // three times as many threads are in flight to hide memory latency.  A warp
 // holds 10 sites (lanes 0-9 colour 0, 10-19 colour 1, 20-29 colour 2).
 //
-// Two kernels on that mapping, bit-identical to each other:
+// Three kernels, bit-identical to each other:
 //   k_hop_df_staged  each thread copies the next direction's seven operands
 //                    into shared memory with cp.async while it computes the
 //                    current one with the packed (re, im) arithmetic of
-//                    wd_df2.cuh (half the instructions); the default;
+//                    wd_df2.cuh (half the instructions);
+//   k_hop_df_grouped the same staging and arithmetic with a colour per warp:
+//                    three warps share 32 sites and exchange half-spinors
+//                    through shared memory, so no lane idles (the fastest on
+//                    GB300);
 //   k_hop_df_pipe    scalar arithmetic, the next direction's operands loaded
 //                    into registers ahead of use.
 #include "wd_hop.cuh"
@@ -315,6 +319,107 @@ __global__ void __launch_bounds__(32 * WARPS) k_hop_df_staged(const SplitDF p)
     pair_epilogue(p, x, acc);
 }
 
+// Grouped colour split: three warps per 32 sites, warp w of a group holding
+// colour w of each of its 32 sites, so every lane works (the 10-sites-a-warp
+// split leaves lanes 30-31 idle: 1/16 of the FP32 pipe, which bounds this
+// kernel).  The projected half-spinors go to the partner colours through
+// shared memory instead of by warp shuffles: one named barrier per direction
+// and group, two buffers alternating by direction, so a buffer is rewritten
+// only after every partner has passed the next direction's barrier (and so
+// has finished reading it).  Operands are staged as in df_staged_site and the
+// arithmetic is pair_compute's, in the same order: bit-identical results.
+template <int GROUPS>
+__device__ __forceinline__ SplitCtx group_ctx(const SplitDF &p)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int grp = warp / 3;
+    const int s_raw = (blockIdx.x * GROUPS + grp) * 32 + lane;
+    SplitCtx x;
+    x.on = s_raw < p.g.Vh;
+    x.col = warp - 3 * grp;
+    x.s = x.on ? s_raw : 0;
+    x.c1 = x.col == 2 ? 0 : x.col + 1;
+    x.c2 = x.col == 0 ? 2 : x.col - 1;
+    x.src1 = (3 * grp + x.c1) * 32 + lane;  // partner threads in the block
+    x.src2 = (3 * grp + x.c2) * 32 + lane;
+    x.cs = wd_site(p.g, x.s, p.cb);
+    return x;
+}
+
+__device__ __forceinline__ float4 dfp_raw(const dfp &v) { return make_float4(v.h.x, v.h.y, v.l.x, v.l.y); }
+__device__ __forceinline__ dfp dfp_unraw(float4 v) { return dfp{make_float2(v.x, v.y), make_float2(v.z, v.w)}; }
+
+// xb: this direction's exchange buffer, h0 of every thread then h1 (T threads)
+template <int MU, bool FWD, bool DAG, int T>
+__device__ __forceinline__ void group_compute(const SplitCtx &x, const DirLoadP &L, float4 *xb, dfp *acc)
+{
+    constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
+    dfp h0, h1;
+    wd_proj1<MU, SG>(L.s[0], L.s[1], L.s[2], L.s[3], h0, h1);
+    xb[threadIdx.x] = dfp_raw(h0);
+    xb[T + threadIdx.x] = dfp_raw(h1);
+    asm volatile("bar.sync %0, 96;" ::"r"(1 + (int)(threadIdx.x >> 5) / 3) : "memory");
+    const dfp h0b = dfp_unraw(xb[x.src1]), h1b = dfp_unraw(xb[T + x.src1]);
+    const dfp h0c = dfp_unraw(xb[x.src2]), h1c = dfp_unraw(xb[T + x.src2]);
+    dfp t0, t1;
+    if constexpr (FWD) {
+        t0 = c_madd(c_madd(c_mul(L.w[0], h0), L.w[1], h0b), L.w[2], h0c);
+        t1 = c_madd(c_madd(c_mul(L.w[0], h1), L.w[1], h1b), L.w[2], h1c);
+    } else {
+        t0 = c_maddc(c_maddc(c_mulc(L.w[0], h0), L.w[1], h0b), L.w[2], h0c);
+        t1 = c_maddc(c_maddc(c_mulc(L.w[0], h1), L.w[1], h1b), L.w[2], h1c);
+    }
+    wd_recon1<MU, SG>(t0, t1, acc[0], acc[1], acc[2], acc[3]);
+}
+
+template <int D, bool DAG, int T, bool LCG>
+__device__ __forceinline__ void group_step(const SplitDF &p, const SplitCtx &x, float4 *base, float4 *xch, dfp *acc)
+{
+    constexpr int NS = 2;
+    if constexpr (D + 1 < 8) stage_issue<D + 1, LCG>(p, x, base + ((D + 1) % NS) * kOps * T, T);
+    wd_cp_async_commit();  // possibly empty: one group per step keeps the count
+    wd_cp_async_wait<1>();
+    DirLoadP L;
+    const float4 *slot = base + (D % NS) * kOps * T;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) L.s[k] = dfp_from_f4(slot[k * T]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) L.w[k] = dfp_from_f4(slot[(4 + k) * T]);
+    group_compute<D / 2, (D % 2) == 0, DAG, T>(x, L, xch + (D & 1) * 2 * T, acc);
+}
+
+// this thread's colour of the hopping sum at its site (grouped split)
+template <bool DAG, int GROUPS, bool LCG>
+__device__ __forceinline__ void df_group_site(const SplitDF &p, const SplitCtx &x, dfp *acc)
+{
+    constexpr int T = 96 * GROUPS;
+    __shared__ float4 slots[2 * kOps * T];
+    __shared__ float4 xch[2 * 2 * T];
+    float4 *base = slots + threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) acc[k] = c_zero(dfp());
+    stage_issue<0, LCG>(p, x, base, T);
+    wd_cp_async_commit();
+    group_step<0, DAG, T, LCG>(p, x, base, xch, acc);
+    group_step<1, DAG, T, LCG>(p, x, base, xch, acc);
+    group_step<2, DAG, T, LCG>(p, x, base, xch, acc);
+    group_step<3, DAG, T, LCG>(p, x, base, xch, acc);
+    group_step<4, DAG, T, LCG>(p, x, base, xch, acc);
+    group_step<5, DAG, T, LCG>(p, x, base, xch, acc);
+    group_step<6, DAG, T, LCG>(p, x, base, xch, acc);
+    group_step<7, DAG, T, LCG>(p, x, base, xch, acc);
+}
+
+// GROUPS groups a block, registers capped for MINB blocks per SM
+template <bool DAG, int GROUPS, bool LCG, int MINB>
+__global__ void __launch_bounds__(96 * GROUPS, MINB) k_hop_df_grouped(const SplitDF p)
+{
+    const SplitCtx x = group_ctx<GROUPS>(p);
+    dfp acc[4];
+    df_group_site<DAG, GROUPS, LCG>(p, x, acc);
+    pair_epilogue(p, x, acc);
+}
+
 // The reliable update's second Schur hop fused with the true residual
 // (wd_hop_hi_residual): s = bhat - (alpha acc + beta x) in double-float,
 // rounded to FP32 into s32 (plane c/2, half c&1 of the float4 for component
@@ -327,12 +432,15 @@ struct ResSinkDF {
     double *result;
 };
 
-template <int WARPS, bool LCG>
-__global__ void __launch_bounds__(32 * WARPS) k_hop_df_res(const SplitDF p, const ResSinkDF r)
+// WARPS warps of the 10-sites-a-warp split, or (GROUPED) WARPS / 3 groups of
+// the grouped split
+template <int WARPS, bool LCG, bool GROUPED = false, int MINB = 0>
+__global__ void __launch_bounds__(32 * WARPS, MINB) k_hop_df_res(const SplitDF p, const ResSinkDF r)
 {
-    const SplitCtx x = split_ctx<WARPS>(p);
+    const SplitCtx x = GROUPED ? group_ctx<WARPS / 3>(p) : split_ctx<WARPS>(p);
     dfp acc[4];
-    df_staged_site<false, WARPS, 1, 2, LCG>(p, x, acc);
+    if constexpr (GROUPED) df_group_site<false, WARPS / 3, LCG>(p, x, acc);
+    else df_staged_site<false, WARPS, 1, 2, LCG>(p, x, acc);
     float n = 0.f;
     if (x.on) {
         const size_t Vh = p.g.Vh;
@@ -412,7 +520,12 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
     //   2  staged, 2 warps, links through L1       386.2 / 127.0 us
     //   3  register-pipelined scalar, 2 warps      459.9 / 150.1 us
     //   4  register-pipelined scalar, 4 warps      459.0 / 149.5 us
-    // Dropped (same lattices): the staged form two directions ahead in three
+    //   5  grouped split, 2 groups, 4 blocks/SM    345.8 us (1.741 ms at 48^3x96 against 1.900 for 0)
+    // Dropped (same lattices): the grouped split with 1 group (389 us), 2
+    // groups without the register cap (96 registers, 353 us) or 4 groups
+    // (414 us), and with a split-phase exchange on mbarriers (arrive, own
+    // colour's term, bounded wait: 375 us, the polling costs more issue slots
+    // than the barrier stalls it removes); the staged form two directions ahead in three
     // slots (413 / 135 us with L2-only links, 584 / 196 us through L1: the
     // larger shared-memory footprint leaves less L1 for the neighbour
     // spinors); staged with registers capped at 80 or 72 (420 and 635 us,
@@ -422,15 +535,24 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
     // unbounded colour-split form (242 registers); the register-prefetching
     // packed form; the scalar pipelined form capped at 80 or 72 registers
     // (550-830 bytes of spills, 639 and 778 us).
+    // the grouped split: 2 groups (192 threads), registers capped for 4 blocks per SM
+    auto run_grouped = [&]() -> wd_status {
+        const int blocks = (lat->g.Vh + 63) / 64;
+        if (dag) k_hop_df_grouped<true, 2, true, 4><<<blocks, 192, 0, ctx->stream>>>(p);
+        else k_hop_df_grouped<false, 2, true, 4><<<blocks, 192, 0, ctx->stream>>>(p);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    };
     using F = std::false_type;
     using T = std::true_type;
     using W2 = std::integral_constant<int, 2>;
     using W4 = std::integral_constant<int, 4>;
-    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 5, [&](int v) -> wd_status {
+    return wd_tune_launch(ctx, "hop_df64", lat->g.Vh, 6, [&](int v) -> wd_status {
         if (v == 1) return run_staged(W2(), T());
         if (v == 2) return run_staged(W2(), F());
         if (v == 3) return run_pipe(W2());
         if (v == 4) return run_pipe(W4());
+        if (v == 5) return run_grouped();
         return run_staged(W4(), T());
     });
 }
@@ -460,8 +582,14 @@ wd_status wd_hop_df_residual(wd_context *ctx, const wd_lattice *lat, const float
         WD_LAUNCHED(ctx);
         return WD_OK;
     };
-    // the plain double-float hop's tuned shape among the staged variants
+    // the plain double-float hop's tuned shape (its register-pipelined
+    // variants 3 and 4 take variant 0's)
     const int v = wd_tune_choice(ctx, "hop_df64", lat->g.Vh);
+    if (v == 5) {  // the grouped split (2 groups, 4 blocks per SM)
+        k_hop_df_res<6, true, true, 4><<<(lat->g.Vh + 63) / 64, 192, 0, ctx->stream>>>(p, r);
+        WD_LAUNCHED(ctx);
+        return WD_OK;
+    }
     if (v == 1) return run(std::integral_constant<int, 2>(), std::true_type());
     if (v == 2) return run(std::integral_constant<int, 2>(), std::false_type());
     return run(std::integral_constant<int, 4>(), std::true_type());

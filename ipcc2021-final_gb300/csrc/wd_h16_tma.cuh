@@ -17,16 +17,14 @@
 // direction order, so results are bit-identical to the other FP16 kernels.
 // Links have no reuse between sites and are loaded per thread.
 //
-// Every wait on a barrier is bounded: after kTmaWaitNs (0.5 s) the thread
+// Every wait on a barrier is bounded (wd_mbar.cuh, 0.5 s): after that the thread
 // sets *err, waits once more (bounded) for copies still in flight and returns
 // without computing, so a copy that never completes cannot hang the GPU; the
 // host reports the flag as an error (wd_context_device_check).
 #pragma once
 #include <cuda.h>
 #include "wd_h16m.cuh"
-
-constexpr unsigned long long kTmaWaitNs = 500000000ull;  // 0.5 s: copies take microseconds
-constexpr long long kTmaWaitPolls = 1ll << 26;
+#include "wd_mbar.cuh"
 
 // shared-memory regions: spinor planes of the tile (0) and of the faces y-,
 // y+, z-, z+, t-, t+ (1..6); their scales (7..13)
@@ -47,8 +45,6 @@ struct H16TmaArgs {
     int *err;  // set when a wait gives up
 };
 
-__device__ __forceinline__ unsigned wd_smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
 __device__ __forceinline__ void wd_tma_load4(unsigned dst, const CUtensorMap *m, int c0, int c1, int c2, int c3,
                                              unsigned mbar)
 {
@@ -66,31 +62,6 @@ __device__ __forceinline__ void wd_tma_load5(unsigned dst, const CUtensorMap *m,
         "%6}], [%7];" ::"r"(dst),
         "l"(m), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(mbar)
         : "memory");
-}
-
-__device__ __forceinline__ unsigned long long wd_globaltimer_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// true once phase `parity` of the mbarrier has completed; false after
-// kTmaWaitNs of wall time (or kTmaWaitPolls polls, whichever comes first)
-__device__ __forceinline__ bool wd_mbar_wait(unsigned mbar, unsigned parity)
-{
-    const unsigned long long t0 = wd_globaltimer_ns();
-    for (long long i = 0; i < kTmaWaitPolls; ++i) {
-        unsigned done;
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if (wd_globaltimer_ns() - t0 > kTmaWaitNs) return false;
-    }
-    return false;
 }
 
 // The operands of direction D for the thread at half-x index xh, tile rows
