@@ -50,3 +50,34 @@ def test_variants_bit_identical(wd, oracle, case, prec, kernel, bar):
             wd.tune_pin(kernel, vh, n)
     finally:
         wd.tune_pin(kernel, vh, -1)
+
+
+@pytest.mark.parametrize("dims", [(16, 8, 8, 8), (12, 6, 10, 4)])
+def test_df64_grouped_split_in_solver(wd, oracle, ctx, dims):
+    """The double-float hop's grouped colour split (variant 5: a colour per
+    warp, half-spinors exchanged through shared memory) also drives the
+    reliable update's fused residual kernel: the mixed FP16 solve with
+    double-float reliable updates gives the same solution, bit for bit, with
+    variant 5 pinned as with variant 0, and it matches the oracle.  The second
+    lattice leaves a partial last group (Vh = 1440 = 22.5 x 64)."""
+    gauge = wd.gen_gauge(dims, seed=12)
+    src = wd.gen_source(dims, seed=12)
+    lat = ctx.lattice(dims, gauge)
+    vh = int(np.prod(dims)) // 2
+    want, _, _ = oracle.cg_eo(src, gauge, dims, 0.05, tol=1e-12)
+    sols = {}
+    try:
+        for v in (0, 5):
+            wd.tune_pin("hop_df64", vh, v)
+            b, x = lat.field(src), lat.field()
+            p = wd.solver_params(kind=wd.CG_EO, mass=0.05, tol=1e-10, max_iter=5000, prec=wd.F16,
+                                 prec_reliable=wd.DF64)
+            st = lat.solve(b, x, p)
+            assert st.reliable_updates >= 2
+            sols[v] = x.download()
+            assert rel_l2(sols[v], want) < 1e-8, v
+            b.close()
+            x.close()
+        assert np.array_equal(sols[0], sols[5])
+    finally:
+        wd.tune_pin("hop_df64", vh, -1)
