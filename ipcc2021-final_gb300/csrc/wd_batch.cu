@@ -40,7 +40,7 @@ namespace {
 
 constexpr int kSites = 32;  // sites per warp (one system per warp)
 constexpr int kChunk = 8192;     // sites per xpay chunk (one block each)
-constexpr int kBatchHopVariants = 5;
+constexpr int kBatchHopVariants = 6;
 constexpr int kMaxPerGraph = 8;  // iterations queued per graph launch at most
 
 struct BGroup {
@@ -717,13 +717,19 @@ wd_status BatchEngine::graph(int k, cudaGraphExec_t *exec)
 }
 
 // batched hop h (operand table h) with launch variant v and epilogue epi:
-// (systems per block, min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12), (4, none).
-// A whole 24-source solve at 24^3x48 before the epilogue fusion (GB300,
-// seconds): FP32 inner 0.298 / 0.270 / 0.265 / 0.268 / 0.274, FP16 inner
-// 0.263 / 0.247 / 0.244 / 0.245 / 0.256.  Dropped: the hop with each thread's
-// operands staged in shared memory by cp.async, with 4 or 2 systems per block
-// (FP32 0.276 / 0.279, FP16 0.243 / 0.243: no gain; the block's systems
-// already share links through L1).
+// (systems per block, min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12),
+// (4, none), (4, 8).  A whole 24-source solve at 24^3x48 before the epilogue
+// fusion (GB300, seconds): FP32 inner 0.298 / 0.270 / 0.265 / 0.268 / 0.274,
+// FP16 inner 0.263 / 0.247 / 0.244 / 0.245 / 0.256.  The last, registers
+// capped at 64 for 32 warps per SM (a few spilled registers; the kernel is
+// bound by L2 latency, so more warps in flight pay): the plain hop at
+// 24 x 24^3x48 0.604 ms (FP32) / 0.450 ms (FP16) against 0.632 / 0.498 for
+// (4, 6) (the tuner's timings), the tuner's choice at every batch size
+// measured, and whole batched solves 1-4 % faster.  Dropped: (8, 4) at 64
+// registers (0.610 / 0.456 ms);
+// the hop with each thread's operands staged in shared memory by cp.async,
+// with 4 or 2 systems per block (FP32 0.276 / 0.279, FP16 0.243 / 0.243 s: no
+// gain; the block's systems already share links through L1).
 wd_status BatchEngine::hop(int h, int cb, int dag, int v, int epi)
 {
     const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_sc_.p, d_partial_.p, cb};
@@ -760,6 +766,7 @@ wd_status BatchEngine::hop(int h, int cb, int dag, int v, int epi)
     case 2: return run(I4(), std::integral_constant<int, 6>());
     case 3: return run(I2(), std::integral_constant<int, 12>());
     case 4: return run(I4(), I0());
+    case 5: return run(I4(), std::integral_constant<int, 8>());
     default: return run(I8(), I0());
     }
 }
