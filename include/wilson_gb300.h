@@ -66,16 +66,22 @@ void *wd_context_stream(wd_context *ctx);
 /* Device kernels launched on this context since creation (bookkeeping for benchmarks). */
 uint64_t wd_context_launches(const wd_context *ctx);
 /* Wait for the context's stream, then report (and clear) the device-side
- * error flag: WD_ERR_CUDA if a kernel's bounded wait gave up since the last
- * check (the TMA-staged FP16 hopping kernel waits on its copies with an
- * iteration limit, after which the block writes nothing and sets the flag;
- * its output is then undefined), else WD_OK. */
+ * error flag: WD_ERR_TIMEOUT if a kernel's bounded wait gave up since the
+ * last check (the TMA-staged FP16 hopping kernel waits on its copies for at
+ * most 0.5 s, after which the block writes nothing and sets the flag; its
+ * output is then undefined), else WD_OK. */
 wd_status wd_context_device_check(wd_context *ctx);
 /* Testing aid, host-side failure injection: after n more successful field or
  * work-buffer allocations on this context, the next ones fail with
  * WD_ERR_OOM; n < 0 turns it off (the default).  Returns the previous
  * setting (the allocations left before failing, or -1). */
 int wd_debug_fail_allocations_after(wd_context *ctx, int n);
+/* Testing aid for the bounded device waits: one warp waits on a shared-memory
+ * barrier that nothing completes; the wait gives up after its bound (0.5 s)
+ * and sets the device error flag, as a kernel whose copies never landed
+ * would, so the next wd_context_device_check returns WD_ERR_TIMEOUT.
+ * *waited_seconds: how long the wait ran, as the device's timer measured it. */
+wd_status wd_debug_expire_wait(wd_context *ctx, double *waited_seconds);
 
 /* ---- gauge field (replaces lattice_gauge, include/lattice_gauge.h:11-26) ---- */
 /* Upload four reference-layout link arrays (each V*9 complex doubles).

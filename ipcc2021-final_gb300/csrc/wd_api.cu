@@ -180,7 +180,7 @@ extern "C" wd_status wd_context_device_check(wd_context *ctx)
     WD_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (!flag) return WD_OK;
     WD_CUDA(ctx, cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
-    return wd_fail(ctx, WD_ERR_CUDA, "a kernel's bounded wait gave up (TMA copies did not complete)");
+    return wd_fail(ctx, WD_ERR_TIMEOUT, "a kernel's bounded device wait gave up (its output is undefined)");
 }
 
 extern "C" int wd_debug_fail_allocations_after(wd_context *ctx, int n)

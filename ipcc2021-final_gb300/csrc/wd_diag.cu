@@ -1,9 +1,27 @@
 // wd_diag.cu -- device throughput probe: independent FMA chains in FP64 and
 // FP32, timed with CUDA events.  Gives the compute roof the hopping kernels
 // are compared against (the FP64 pipe of GB300 is far narrower than FP32).
+// Also a testing aid for the bounded device waits (wd_debug_expire_wait).
 #include "wd_kernels.h"
+#include "wd_mbar.cuh"
 
 namespace {
+// One warp waits on a barrier nothing arrives at: the bounded wait gives up
+// and the kernel records it in the device error flag.
+__global__ void __launch_bounds__(32) k_expire_wait(int *err, unsigned long long *waited_ns)
+{
+    __shared__ unsigned long long bar;
+    const unsigned mbar = wd_smem_u32(&bar);
+    if (threadIdx.x == 0) wd_mbar_init(mbar, 1);
+    __syncwarp();
+    const unsigned long long t0 = wd_globaltimer_ns();
+    const bool done = wd_mbar_wait(mbar, 0);
+    if (threadIdx.x == 0) {
+        if (!done) atomicExch(err, 1);
+        *waited_ns = wd_globaltimer_ns() - t0;
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_fma_chains(T *out, int iters, T a, T b)
 {
@@ -57,5 +75,21 @@ extern "C" wd_status wd_diag_fma_peak(wd_context *ctx, double *fp64_tflops, doub
     if (e != cudaSuccess) return wd_cuda_check(ctx, e, "fma probe");
     *fp64_tflops = best64;
     *fp32_tflops = best32;
+    return WD_OK;
+}
+
+extern "C" wd_status wd_debug_expire_wait(wd_context *ctx, double *waited_seconds)
+{
+    if (!ctx || !waited_seconds) return wd_fail(ctx, WD_ERR_BAD_ARG, "null argument");
+    unsigned long long *d = nullptr, ns = 0;
+    WD_CUDA(ctx, cudaMalloc(&d, sizeof(unsigned long long)));
+    k_expire_wait<<<1, 32, 0, ctx->stream>>>(ctx->dev_err, d);
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&ns, d, sizeof(ns), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return wd_cuda_check(ctx, e, "bounded-wait probe");
+    *waited_seconds = (double)ns * 1e-9;
     return WD_OK;
 }

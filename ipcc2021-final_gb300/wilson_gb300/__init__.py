@@ -74,6 +74,7 @@ def _load() -> C.CDLL:
         "wd_context_stream": (vp, [vp]),
         "wd_context_launches": (C.c_uint64, [vp]),
         "wd_context_device_check": (C.c_int, [vp]),
+        "wd_debug_expire_wait": (C.c_int, [vp, C.POINTER(C.c_double)]),
         "wd_debug_fail_allocations_after": (C.c_int, [vp, C.c_int]),
         "wd_lattice_create": (C.c_int, [vp, ip, d4, C.POINTER(vp)]),
         "wd_lattice_update": (C.c_int, [vp, vp, d4]),
@@ -258,8 +259,15 @@ class Context:
         return int(lib.wd_context_launches(self.handle))
 
     def device_check(self) -> None:
-        """Wait for the stream and raise if a kernel's bounded wait gave up."""
+        """Wait for the stream and raise (TIMEOUT) if a kernel's bounded wait gave up."""
         self.check(lib.wd_context_device_check(self.handle))
+
+    def debug_expire_wait(self) -> float:
+        """Testing aid: run a device wait that can only give up (after its
+        0.5 s bound); returns how long it waited, in seconds."""
+        w = C.c_double()
+        self.check(lib.wd_debug_expire_wait(self.handle, C.byref(w)))
+        return w.value
 
     def fail_allocations_after(self, n: int) -> int:
         """Testing aid: the next allocations after n more successful ones fail
