@@ -27,7 +27,8 @@ one lattice per GPU); value = sum over ranks of per-rank work / max time.
 
 --impl reference times the reference's CPU implementation of the same
 application (the oracle's C restatement on all host cores; the reference's
-own AVX2 sources do not build on the Arm host of the GPU machine).
+own AVX2 sources do not build on an Arm host such as a GB300 node's Grace
+CPU).
 """
 from __future__ import annotations
 
@@ -273,7 +274,7 @@ class OracleSolution:
         self.x, self.iterations, self.true_residual = self.orc.cg_eo(src, gauge, dims, mass, tol=1e-14)
         self.seconds = time.perf_counter() - t0
 
-    def judge(self, sol) -> dict:
+    def assess(self, sol) -> dict:
         """Error of a GPU solution against this one, and its FP64 true residual
         recomputed by the oracle."""
         r = self.src - self.orc.dslash_full(sol, self.gauge, self.dims, self.mass, 0)
@@ -323,7 +324,7 @@ def solver_bench(wd, ctx, lat, src, mass: float, tol: float = 1e-10, plans=SOLVE
                      "reliable_updates": st.reliable_updates, "true_residual": st.true_residual,
                      "rel_diff_vs_f64": float(np.linalg.norm(sol - ref) / np.linalg.norm(ref))}
         if oracle_sol is not None:
-            out[name].update(oracle_sol.judge(sol))
+            out[name].update(oracle_sol.assess(sol))
         x.close()
     if "f64" in out:
         for name in out:

@@ -2,9 +2,9 @@
  * wilson_oracle.c -- TEST INFRASTRUCTURE ONLY.
  *
  * Plain-C restatement of the reference Wilson-fermion operator and CG solver
- * (CHN-ChenYi/IPCC2021-Final).  It is the checker for the CUDA library: only
- * the tests, the smoke check and the CPU-baseline leg of the benchmark load
- * it.  Nothing in the product links against it.
+ * (CHN-ChenYi/IPCC2021-Final).  It is the oracle the CUDA library is tested
+ * against: only the tests, the smoke check and the CPU-baseline leg of the
+ * benchmark load it.  Nothing in the product links against it.
  *
  * Parity pinning: this restatement is checked against golden vectors written
  * by the reference's own sources (compiled single-rank), stored under
