@@ -344,7 +344,9 @@ bool launch_hop_h16_tma(wd_context *ctx, const P &p, int dag, wd_status *st)
 // 32^3x64: all within 1 % of 102.5 us).  FP16: the FP16-operand kernel
 // (wd_h16m.cuh) with each thread's next-direction operands staged in shared
 // memory by cp.async, 128 threads (6 blocks per SM) or 64 (12), registers
-// capped at 80: 63.8 / 63.8 us at 32^3x64, 0.291 / 0.293 ms at 48^3x96; or
+// capped at 80: 63.8 / 63.8 us at 32^3x64, 0.291 / 0.293 ms at 48^3x96; 128
+// threads capped at 64 registers for 8 blocks per SM (variant 3, a few bytes
+// spilled): 63.6 us and 0.289 ms; or
 // the TMA-staged kernel (wd_h16_tma.cuh; 75.8 us and 0.358 ms: every block
 // stalls on its copies before its first direction, and at 3 blocks of 256
 // threads an SM that start-up is not hidden -- issue slots busy 64 % against
@@ -363,7 +365,7 @@ template <class Sp, class Lk>
 wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p, int dag)
 {
     constexpr bool kF16 = std::is_same_v<Sp, SpF16>;
-    return wd_tune_launch(ctx, name, p.g.Vh, kF16 ? 3 : 4, [&](int v) -> wd_status {
+    return wd_tune_launch(ctx, name, p.g.Vh, 4, [&](int v) -> wd_status {
         auto make = [&](auto threads, auto minb) {
             HopLP<Sp, Lk, decltype(threads)::value, decltype(minb)::value> q;
             q.g = p.g, q.cb = p.cb, q.in = p.in, q.out = p.out, q.x = p.x, q.link = p.link;
@@ -380,6 +382,7 @@ wd_status launch_tuned(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &p
                 v = 0;  // the lattice does not fit the TMA kernel
             }
             if (v == 1) return launch_hop_h16m(ctx, make(T64(), std::integral_constant<int, 12>()), dag);
+            if (v == 3) return launch_hop_h16m(ctx, make(T128(), std::integral_constant<int, 8>()), dag);
             return launch_hop_h16m(ctx, make(T128(), std::integral_constant<int, 6>()), dag);
         } else {
             switch (v) {

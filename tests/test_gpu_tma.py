@@ -48,7 +48,7 @@ def test_tma_variants_bit_identical(wd, ctx, oracle, dims):
     fi = lat.field(src, prec=wd.F16)
     vh = int(np.prod(dims)) // 2
     lat.dslash_offd(fi, lat.field(prec=wd.F16), 0, 0, wd.F16)  # registers the variant count
-    assert wd.tune_variants("hop_f16") == 3
+    assert wd.tune_variants("hop_f16") >= 3  # variant 2 is the TMA-staged kernel
     try:
         base = _run_all(wd, ctx, lat, fi, dims, 0)
         for (kind, dag, *cb), got in base.items():
