@@ -625,9 +625,12 @@ def run_ours(args) -> None:
         n_e2e = max(3, min(args.steps, 20))
         barrier()
         t0 = time.perf_counter()
+        per_call = []
         for _ in range(n_e2e):
+            tc = time.perf_counter()
             ctx.check(wd.lib.wd_host_dslash_offd(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
                                                  wd._ptr(h_src), wd._ptr(h_dst), 0, 0))
+            per_call.append(time.perf_counter() - tc)
         e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e, world)
         # DslashNew (full M) through its host-buffer entry point, same buffers
         ctx.check(wd.lib.wd_host_dslash_full(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
@@ -640,6 +643,9 @@ def run_ours(args) -> None:
         e2e = {"value": replica_throughput(BYTES_PER_SITE_F64 * vh, e2e_s, world) / 1e9, "unit": "GB/s",
                "h2d_bytes_per_step": int(src.nbytes // 2), "d2h_bytes_per_step": int(src.nbytes // 2),
                "steps": n_e2e, "ms_per_step": e2e_s * 1e3, "dslash_new_host_ms": full_ms,
+               "ms_per_call_min_median_max": [round(1e3 * min(per_call), 4),
+                                              round(1e3 * float(np.median(per_call)), 4),
+                                              round(1e3 * max(per_call), 4)],
                "path": "wd_host_dslash_offd (DslashoffdNew): the source parity it reads goes up and the "
                        "computed parity comes back in up to 16 time-slab chunks overlapped with compute on "
                        "two streams, the kernel working on the reference's site-major layout in the staging "
