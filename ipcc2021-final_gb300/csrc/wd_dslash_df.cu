@@ -523,9 +523,12 @@ wd_status wd_hop_df(wd_context *ctx, const wd_lattice *lat, const float4 *in_blo
     //   5  grouped split, 2 groups, 4 blocks/SM    345.8 us (1.741 ms at 48^3x96 against 1.900 for 0)
     // Dropped (same lattices): the grouped split with 1 group (389 us), 2
     // groups without the register cap (96 registers, 353 us) or 4 groups
-    // (414 us), and with a split-phase exchange on mbarriers (arrive, own
+    // (414 us), with a split-phase exchange on mbarriers (arrive, own
     // colour's term, bounded wait: 375 us, the polling costs more issue slots
-    // than the barrier stalls it removes); the staged form two directions ahead in three
+    // than the barrier stalls it removes), and with the half-spinors passed
+    // through the thread's just-read staging slot so that 5 blocks fit an SM
+    // (64 registers, 80 bytes spilled, the next copies issued behind each
+    // barrier: 383 us); the staged form two directions ahead in three
     // slots (413 / 135 us with L2-only links, 584 / 196 us through L1: the
     // larger shared-memory footprint leaves less L1 for the neighbour
     // spinors); staged with registers capped at 80 or 72 (420 and 635 us,
