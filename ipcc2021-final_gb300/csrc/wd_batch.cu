@@ -40,7 +40,7 @@ namespace {
 
 constexpr int kSites = 32;  // sites per warp (one system per warp)
 constexpr int kChunk = 8192;     // sites per xpay chunk (one block each)
-constexpr int kBatchHopVariants = 6;
+constexpr int kBatchHopVariants = 7;
 constexpr int kMaxPerGraph = 8;  // iterations queued per graph launch at most
 
 struct BGroup {
@@ -203,23 +203,39 @@ __device__ __forceinline__ auto batch_policy(const BTable &t, const BGroup &G, c
 // SYS systems (warps) per block sharing the block's 32 sites; MINB blocks per
 // SM (0: no bound) bound the registers.  A warp is one system's 32
 // consecutive sites, so a reducing epilogue writes one partial per warp.
-template <bool DAG, bool F16, int SYS, int MINB, int EPI>
+// R2 (FP16 storage): row 2 of the block's links is rebuilt once per site and
+// direction into shared memory by all the block's warps together, and every
+// system reads it there instead of rebuilding it (the same values).
+template <bool DAG, bool F16, int SYS, int MINB, int EPI, bool R2 = false>
 __global__ void __launch_bounds__(kSites * SYS, MINB) k_batch_hop(const BTable t)
 {
     const int gi = find_group(t.groups, t.ngroups, blockIdx.x);
     const BGroup &G = t.groups[gi];
     const int r = blockIdx.y * SYS + (threadIdx.x / kSites);
+    const int blk = blockIdx.x - G.block_start;
+    const int lane = threadIdx.x % kSites;
+    const int s = blk * kSites + lane;
+    static_assert(!R2 || F16, "the shared row-2 table is for 12-real FP16 links");
+    __shared__ unsigned r2[R2 ? 8 : 1][3][kSites];
+    if constexpr (R2) {
+        // every warp takes part, whether or not its system iterates
+        if (s < G.g.Vh) {
+            const uint4 *a = (const uint4 *)G.gauge;
+            const LinkF16 lk{a, (const uint2 *)(a + (size_t)8 * G.g.Vh), G.g.Vh};
+            h16_fill_row2<SYS>(G.g, t.cb, lk, s, r2, threadIdx.x / kSites, lane);
+        }
+        __syncthreads();
+    }
     if (r >= G.nsys) return;  // whole warps
     const int sys = G.first_sys + r;
     if (!t.sc[sys].active) return;
-    const int blk = blockIdx.x - G.block_start;
-    const int s = blk * kSites + (threadIdx.x % kSites);
     const BSys &S = t.sys[sys];
     float v = 0.f;
     if (s < G.g.Vh) {
         float2 acc[12];
         // FP16 storage: the FP16-operand arithmetic of the solo FP16 kernel
-        if constexpr (F16) h16_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
+        if constexpr (R2) h16_hop_site_r2<DAG>(batch_policy<F16>(t, G, S), s, r2, lane, acc);
+        else if constexpr (F16) h16_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
         else wd_hop_site<DAG>(batch_policy<F16>(t, G, S), s, acc);
         v = batch_epilogue<F16, EPI>(t, S, sys, s, G.g.Vh, acc);
     }
@@ -718,14 +734,18 @@ wd_status BatchEngine::graph(int k, cudaGraphExec_t *exec)
 
 // batched hop h (operand table h) with launch variant v and epilogue epi:
 // (systems per block, min blocks per SM) = (8, none), (8, 3), (4, 6), (2, 12),
-// (4, none), (4, 8).  A whole 24-source solve at 24^3x48 before the epilogue
+// (4, none), (4, 8), (4, 8) with the shared row-2 table.  A whole 24-source solve at 24^3x48 before the epilogue
 // fusion (GB300, seconds): FP32 inner 0.298 / 0.270 / 0.265 / 0.268 / 0.274,
 // FP16 inner 0.263 / 0.247 / 0.244 / 0.245 / 0.256.  The last, registers
 // capped at 64 for 32 warps per SM (a few spilled registers; the kernel is
 // bound by L2 latency, so more warps in flight pay): the plain hop at
 // 24 x 24^3x48 0.604 ms (FP32) / 0.450 ms (FP16) against 0.632 / 0.498 for
 // (4, 6) (the tuner's timings), the tuner's choice at every batch size
-// measured, and whole batched solves 1-4 % faster.  Dropped: (8, 4) at 64
+// measured, and whole batched solves 1-4 % faster.  Variant 6, FP16 links:
+// (4, 8) with row 2 of the block's links rebuilt once per site and direction
+// into shared memory and read by all four systems (k_batch_hop's R2): 0.437
+// against 0.450 ms, the tuner's choice from 24 x 16^3x32 systems up (for
+// FP32 links variant 6 is variant 5's launch).  Dropped: (8, 4) at 64
 // registers (0.610 / 0.456 ms);
 // the hop with each thread's operands staged in shared memory by cp.async,
 // with 4 or 2 systems per block (FP32 0.276 / 0.279, FP16 0.243 / 0.243 s: no
@@ -733,14 +753,15 @@ wd_status BatchEngine::graph(int k, cudaGraphExec_t *exec)
 wd_status BatchEngine::hop(int h, int cb, int dag, int v, int epi)
 {
     const BTable t{d_groups_.p, ngroups_, d_sys_[h].p, d_alpha_[h].p, d_beta_[h].p, d_sc_.p, d_partial_.p, cb};
-    auto run = [&](auto sys, auto minb) -> wd_status {
+    auto run = [&](auto sys, auto minb, auto share) -> wd_status {
         constexpr int S = decltype(sys)::value, M = decltype(minb)::value;
         const dim3 grid(grid_x_, (max_group_sys_ + S - 1) / S);
         auto go = [&](auto f16, auto e) {
             constexpr bool F = decltype(f16)::value;
             constexpr int E = decltype(e)::value;
-            if (dag) k_batch_hop<true, F, S, M, E><<<grid, kSites * S, 0, ctx_->stream>>>(t);
-            else k_batch_hop<false, F, S, M, E><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+            constexpr bool R = F && decltype(share)::value;  // the shared row-2 table: FP16 links only
+            if (dag) k_batch_hop<true, F, S, M, E, R><<<grid, kSites * S, 0, ctx_->stream>>>(t);
+            else k_batch_hop<false, F, S, M, E, R><<<grid, kSites * S, 0, ctx_->stream>>>(t);
         };
         using E0 = std::integral_constant<int, kBEpiPlain>;
         using E1 = std::integral_constant<int, kBEpiNorm>;
@@ -761,13 +782,15 @@ wd_status BatchEngine::hop(int h, int cb, int dag, int v, int epi)
     using I4 = std::integral_constant<int, 4>;
     using I8 = std::integral_constant<int, 8>;
     using I0 = std::integral_constant<int, 0>;
+    using N = std::false_type;
     switch (v) {
-    case 1: return run(I8(), std::integral_constant<int, 3>());
-    case 2: return run(I4(), std::integral_constant<int, 6>());
-    case 3: return run(I2(), std::integral_constant<int, 12>());
-    case 4: return run(I4(), I0());
-    case 5: return run(I4(), std::integral_constant<int, 8>());
-    default: return run(I8(), I0());
+    case 1: return run(I8(), std::integral_constant<int, 3>(), N());
+    case 2: return run(I4(), std::integral_constant<int, 6>(), N());
+    case 3: return run(I2(), std::integral_constant<int, 12>(), N());
+    case 4: return run(I4(), I0(), N());
+    case 5: return run(I4(), std::integral_constant<int, 8>(), N());
+    case 6: return run(I4(), std::integral_constant<int, 8>(), std::true_type());
+    default: return run(I8(), I0(), N());
     }
 }
 

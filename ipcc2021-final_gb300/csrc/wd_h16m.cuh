@@ -111,8 +111,8 @@ __device__ __forceinline__ float2 h16_row(const unsigned *U, int a, const unsign
 
 // the terms of one of the eight neighbours: sp = its 12 components (half2
 // bits, index spin*3 + colour), sc its scale, U the link (rows 0, 1; row 2
-// is filled here)
-template <int MU, bool FWD, bool DAG>
+// is filled here, or, ROW2 = false, already filled by the caller)
+template <int MU, bool FWD, bool DAG, bool ROW2 = true>
 __device__ __forceinline__ void h16_dir_terms(const unsigned *sp, float sc, unsigned *U, float2 *acc)
 {
     constexpr int SG = (FWD ? -1 : 1) * (DAG ? -1 : 1);
@@ -126,7 +126,7 @@ __device__ __forceinline__ void h16_dir_terms(const unsigned *sp, float sc, unsi
         h0[k] = wd_h2u(a);
         h1[k] = wd_h2u(b);
     }
-    h16_row2(U);
+    if constexpr (ROW2) h16_row2(U);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float2 t0 = h16_row<FWD>(U, a, h0), t1 = h16_row<FWD>(U, a, h1);
@@ -219,4 +219,87 @@ __device__ __forceinline__ void h16_hop_site(const P &p, int s, float2 *acc)
     h16_dir<5, DAG>(p, s, c, acc);
     h16_dir<6, DAG>(p, s, c, acc);
     h16_dir<7, DAG>(p, s, c, acc);
+}
+
+// Shared-row-2 form (the batched kernel, several systems over the same 32
+// sites): row 2 of the link of direction D at this thread's site is read
+// from r2[D][k][lane], filled once per block by h16_fill_row2, instead of
+// being rebuilt by every system.  Same arithmetic and rounding as h16_dir.
+template <int D, bool DAG, class P>
+__device__ __forceinline__ void h16_dir_r2(const P &p, int s, const WdSite &c, const unsigned (*r2)[3][32],
+                                           int lane, float2 *acc)
+{
+    constexpr int MU = D / 2;
+    constexpr bool FWD = (D % 2) == 0;
+    const int nb = wd_neighbour(p.g, s, c, MU, FWD);
+    const size_t Vh = p.g.Vh;
+    unsigned sp[12], U[9];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const uint4 v = __ldg(p.in.p + (size_t)j * Vh + nb);
+        sp[4 * j] = v.x, sp[4 * j + 1] = v.y, sp[4 * j + 2] = v.z, sp[4 * j + 3] = v.w;
+    }
+    const float sc = __ldg(p.in.scale + nb);
+    const size_t i = (size_t)(MU * 2 + (FWD ? p.cb : 1 - p.cb)) * Vh + (FWD ? s : nb);
+    const uint4 la = __ldg(p.link.a + i);
+    const uint2 lb = __ldg(p.link.b + i);
+    U[0] = la.x, U[1] = la.y, U[2] = la.z, U[3] = la.w, U[4] = lb.x, U[5] = lb.y;
+    U[6] = r2[D][0][lane], U[7] = r2[D][1][lane], U[8] = r2[D][2][lane];
+    h16_dir_terms<MU, FWD, DAG, false>(sp, sc, U, acc);
+}
+
+template <bool DAG, class P>
+__device__ __forceinline__ void h16_hop_site_r2(const P &p, int s, const unsigned (*r2)[3][32], int lane,
+                                                float2 *acc)
+{
+    const WdSite c = wd_site(p.g, s, p.cb);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) acc[k] = make_float2(0.f, 0.f);
+    h16_dir_r2<0, DAG>(p, s, c, r2, lane, acc);
+    h16_dir_r2<1, DAG>(p, s, c, r2, lane, acc);
+    h16_dir_r2<2, DAG>(p, s, c, r2, lane, acc);
+    h16_dir_r2<3, DAG>(p, s, c, r2, lane, acc);
+    h16_dir_r2<4, DAG>(p, s, c, r2, lane, acc);
+    h16_dir_r2<5, DAG>(p, s, c, r2, lane, acc);
+    h16_dir_r2<6, DAG>(p, s, c, r2, lane, acc);
+    h16_dir_r2<7, DAG>(p, s, c, r2, lane, acc);
+}
+
+// Row 2 of the link of direction D at site s (parity cb output), rebuilt as
+// h16_dir_terms rebuilds it, into r2[D][k][lane].
+template <int D>
+__device__ __forceinline__ void h16_fill_row2_dir(const WdGeom &g, int cb, const LinkF16 &link, int s,
+                                                  const WdSite &c, unsigned (*r2)[3][32], int lane)
+{
+    constexpr int MU = D / 2;
+    constexpr bool FWD = (D % 2) == 0;
+    const size_t i = (size_t)(MU * 2 + (FWD ? cb : 1 - cb)) * g.Vh + (FWD ? s : wd_neighbour(g, s, c, MU, false));
+    const uint4 la = __ldg(link.a + i);
+    const uint2 lb = __ldg(link.b + i);
+    unsigned U[9] = {la.x, la.y, la.z, la.w, lb.x, lb.y, 0u, 0u, 0u};
+    h16_row2(U);
+    r2[D][0][lane] = U[6], r2[D][1][lane] = U[7], r2[D][2][lane] = U[8];
+}
+
+// Fill the block's row-2 table for the site of each lane: warp w of NW takes
+// directions w, w + NW, ...
+template <int NW>
+__device__ __forceinline__ void h16_fill_row2(const WdGeom &g, int cb, const LinkF16 &link, int s,
+                                              unsigned (*r2)[3][32], int warp, int lane)
+{
+    const WdSite c = wd_site(g, s, cb);
+#pragma unroll
+    for (int d = 0; d < 8; ++d)
+        if (d % NW == warp) {
+            switch (d) {
+            case 0: h16_fill_row2_dir<0>(g, cb, link, s, c, r2, lane); break;
+            case 1: h16_fill_row2_dir<1>(g, cb, link, s, c, r2, lane); break;
+            case 2: h16_fill_row2_dir<2>(g, cb, link, s, c, r2, lane); break;
+            case 3: h16_fill_row2_dir<3>(g, cb, link, s, c, r2, lane); break;
+            case 4: h16_fill_row2_dir<4>(g, cb, link, s, c, r2, lane); break;
+            case 5: h16_fill_row2_dir<5>(g, cb, link, s, c, r2, lane); break;
+            case 6: h16_fill_row2_dir<6>(g, cb, link, s, c, r2, lane); break;
+            default: h16_fill_row2_dir<7>(g, cb, link, s, c, r2, lane); break;
+            }
+        }
 }
