@@ -623,13 +623,14 @@ def run_ours(args) -> None:
         host_gauge = [torch.from_numpy(g).pin_memory().numpy() for g in gauge]
         ctx.host_dslash_offd(dims, host_gauge, h_src, 0, 0)  # first call uploads the links
         n_e2e = max(3, min(args.steps, 20))
+        # the C call's arguments, built once (a C/C++ caller passes them as they are)
+        c_dims, c_gauge, c_src, c_dst = wd._dims(dims), wd._gauge_ptrs(host_gauge), wd._ptr(h_src), wd._ptr(h_dst)
         barrier()
         t0 = time.perf_counter()
         per_call = []
         for _ in range(n_e2e):
             tc = time.perf_counter()
-            ctx.check(wd.lib.wd_host_dslash_offd(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
-                                                 wd._ptr(h_src), wd._ptr(h_dst), 0, 0))
+            ctx.check(wd.lib.wd_host_dslash_offd(ctx.handle, c_dims, c_gauge, c_src, c_dst, 0, 0))
             per_call.append(time.perf_counter() - tc)
         e2e_s = max_over_ranks((time.perf_counter() - t0) / n_e2e, world)
         # DslashNew (full M) through its host-buffer entry point, same buffers
@@ -637,8 +638,7 @@ def run_ours(args) -> None:
                                              wd._ptr(h_src), wd._ptr(h_dst), MASS, 0))
         t1 = time.perf_counter()
         for _ in range(n_e2e):
-            ctx.check(wd.lib.wd_host_dslash_full(ctx.handle, wd._dims(dims), wd._gauge_ptrs(host_gauge),
-                                                 wd._ptr(h_src), wd._ptr(h_dst), MASS, 0))
+            ctx.check(wd.lib.wd_host_dslash_full(ctx.handle, c_dims, c_gauge, c_src, c_dst, MASS, 0))
         full_ms = (time.perf_counter() - t1) / n_e2e * 1e3
         e2e = {"value": replica_throughput(BYTES_PER_SITE_F64 * vh, e2e_s, world) / 1e9, "unit": "GB/s",
                "h2d_bytes_per_step": int(src.nbytes // 2), "d2h_bytes_per_step": int(src.nbytes // 2),
