@@ -615,6 +615,8 @@ __global__ void __launch_bounds__(P::kThreads, wd_min_blocks<P>::value) k_hop_lp
 }
 
 // the launch shape the tuner chose for the plain hop of this storage and size
+// (FP16's 8-blocks-per-SM shape too: 128 threads like variant 0, so the same
+// reduction partials and bits; mixed FP16 solves 0.8-1.2 % faster with it)
 template <int EPI, class Sp, class Lk>
 wd_status launch_red(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &b, int dag, WdMxDev *dev,
                      double *partial, Sp pvec, SpF32 rs, SpF32 xs, unsigned *counter = nullptr,
@@ -622,7 +624,7 @@ wd_status launch_red(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &b, 
 {
     constexpr bool kF16 = std::is_same_v<Sp, SpF16>;
     int v = wd_tune_choice(ctx, name, b.g.Vh);
-    if (v < 0 || v == 3) v = 0;  // 3 caps registers at 64: the reducing epilogues would spill
+    if (v < 0 || (v == 3 && !kF16)) v = 0;  // FP32 3 caps registers at 64: the reducing epilogues would spill
     auto run = [&](auto threads, auto minb, auto staged) -> wd_status {
         constexpr int TH = decltype(threads)::value, MB = decltype(minb)::value;
         constexpr bool ST = decltype(staged)::value;
@@ -644,6 +646,7 @@ wd_status launch_red(wd_context *ctx, const char *name, const HopLP<Sp, Lk> &b, 
     using No = std::false_type;
     if constexpr (kF16) {
         if (v == 1) return run(T64(), std::integral_constant<int, 12>(), Yes());
+        if (v == 3) return run(T128(), std::integral_constant<int, 8>(), Yes());
         return run(T128(), std::integral_constant<int, 6>(), Yes());
     } else {
         switch (v) {
